@@ -1,0 +1,138 @@
+// gi_common.cuh - types shared by the host orchestration and the kernels of libgpuinflate.
+//
+// The speculative scheme follows gpuzip's gpuinflate (gpuinflate/inflate.cuh:43-68,
+// gpuinflate/gpuinflate.cu:1-17): decoders start at guessed block starts, each runs until it
+// lands exactly on a later start, and writes 16-bit symbols (a byte, or "the byte d back")
+// that are resolved afterwards. What differs is where the work happens: a decoder is a whole
+// warp (uniform control flow, lanes cooperate on tables and stores), a decoder whose buffer
+// fills takes a new extent from a device pool instead of waiting for another round, and the
+// finder tests 32 bit offsets per lane with bit-sliced masks.
+#pragma once
+#include <stdint.h>
+
+namespace gz {
+
+constexpr uint32_t WINDOW = 32768;
+constexpr uint32_t MAX_SYMBOL_OUT = 258;       // most positions one symbol writes
+constexpr uint32_t REF = 255;                  // symbol values above REF: the byte (value - REF) back
+constexpr uint32_t FIRST_RUN_BLOCKS = 65536;   // references before the start are checked at once in these blocks
+constexpr uint32_t LIT = 0x80000000u;          // resolved entry: a byte (low 8 bits); else the position it copies
+
+// where a decoder starts, or a state an extent starts in (inflate.cuh:43-53 has the same three)
+enum : uint8_t { AT_BLOCK = 0, IN_FIXED = 1, IN_DYNAMIC = 2 };
+
+// how a decode ended (the values of inflate.cuh:41)
+enum : int32_t { S_OK = 0, S_DATA = 1, S_OVERFLOW = 2, S_INPUT = 3, S_STOPPED = 4 };
+
+struct Start {
+    uint64_t bit;
+    uint64_t header;  // IN_DYNAMIC: the block's header; AT_BLOCK: = bit; IN_FIXED: unused
+    uint8_t mode;
+    int8_t final;     // BFINAL of the block it is inside: 0, 1, or -1 unknown
+    uint8_t pad[6];
+};
+static_assert(sizeof(Start) == 24, "Start layout");
+
+// a stream (or the current segment of one) inside the device input buffer, in bits of that buffer
+struct StreamDesc {
+    uint64_t end_bit;   // the input ends here: reading past it gives zero bits and an input error
+    uint64_t end_word;  // first 32-bit word past the input (loads from it on return zero)
+    uint64_t stop;      // decoders stop at the first block or symbol boundary at or after this bit
+    int32_t target_end; // the stream's targets are [first target, target_end)
+    int32_t check_refs; // its first job starts the stream: a reference before the start is invalid at once
+};
+
+struct Job {
+    Start start;
+    int32_t stream;
+    int32_t tfirst;     // may land on targets[tfirst .. target_end)
+    uint64_t pool_off;  // its first extent, in 16-bit symbols (a multiple of 32)
+    uint32_t cap;       // the first extent's size (a multiple of 32)
+    uint32_t flags;     // JOB_CHECK_REFS
+};
+constexpr uint32_t JOB_CHECK_REFS = 1;
+
+struct JobResult {
+    uint64_t end_bit;    // where it stopped
+    uint64_t eob_bit;    // just past its first end-of-block code (UINT64_MAX: none)
+    uint64_t out_len;    // symbols written, all extents
+    uint64_t eob_out;    // symbols written before eob_bit
+    Start resume;        // S_OVERFLOW / S_STOPPED: the exact state to go on from
+    int32_t status;
+    int32_t landed;      // target index it landed on, -1: none (end of stream, stop or error)
+    int32_t end_final;   // BFINAL of the block it ended in, -1 unknown
+    uint32_t blocks;     // block headers read
+};
+
+// a run of a job's output in the pool; job k's first extent is extent k
+struct Extent {
+    uint64_t pool_off;
+    uint64_t len;
+    uint64_t cap;
+    Start start;         // the decoder's exact state where the extent begins
+    int32_t next;        // the job's next extent, -1: last
+    int32_t job;
+};
+
+// a stored block the decoder skipped: its bytes go to the pool later, 16 bytes at a time
+struct StoredCopy {
+    uint64_t src;        // byte offset in the device input
+    uint64_t dst;        // symbol offset in the pool
+    uint32_t len;
+    uint32_t pad;
+};
+
+// device counters of one decode launch
+struct Counters {
+    int32_t next_job;
+    int32_t n_ext;
+    int32_t n_stored;
+    int32_t pad;
+    unsigned long long pool_used;
+};
+
+struct DecodeArgs {
+    const uint8_t* in;
+    const StreamDesc* streams;
+    const Job* jobs;
+    const Start* targets;
+    const int32_t* order;   // job order (longest first)
+    int32_t njobs;
+    int32_t ext_cap;
+    int32_t stored_cap;
+    int32_t pad;
+    uint16_t* pool;
+    uint64_t pool_cap;
+    JobResult* res;
+    Extent* ext;
+    StoredCopy* stored;
+    Counters* ctr;
+};
+
+// a run of the segment's output: pool[src .. src+len) goes to output position dst
+struct Piece {
+    uint64_t src;
+    uint64_t dst;
+    uint64_t len;
+};
+
+// launchers (each file owns its kernels)
+void launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
+                 uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, void* stream);
+int decode_blocks_per_sm();
+void launch_decode(const DecodeArgs& a, int grid, void* stream);
+void launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream);
+void launch_absolute(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t W, uint32_t* e32, int* bad,
+                     uint64_t bad_limit, void* stream);
+void launch_window(uint32_t* e32, const uint8_t* window, uint32_t W, void* stream);
+void launch_jump(uint32_t* e32, uint64_t n, const uint32_t* list, uint32_t* next, unsigned* nnext, uint64_t cap,
+                 void* stream);
+void launch_narrow(const uint32_t* e32, uint64_t n, uint8_t* out, void* stream);
+void launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
+                void* stream);
+uint64_t crc_scratch_words(uint64_t n);
+
+// host-side CRC-32 arithmetic (reflected polynomial 0xEDB88320)
+uint32_t crc32_combine_host(uint32_t crc1, uint32_t crc2, uint64_t len2);
+
+}  // namespace gz

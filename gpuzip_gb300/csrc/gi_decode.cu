@@ -1,0 +1,707 @@
+// gi_decode.cu - the speculative decoders.
+//
+// Semantics per job follow the reference's Decoder::run (gpuinflate/inflate.cuh:474-581): start
+// at a block header or inside a block, decode blocks (stored, fixed, dynamic) until the position
+// at a block boundary equals a later target's bit (landing), the stream's final block ends, the
+// stop bit is reached, or the data is invalid; write one 16-bit symbol per output byte, either the
+// byte or REF + d for "the byte d back". Error classes and the points where the input end is
+// checked are the reference's (inflate.cuh:432-441, :515-524, :536-546, :571).
+//
+// The execution model is this file's own. A decoder is a whole warp: all 32 lanes carry the same
+// bit-reader state and take the same branches, so nothing diverges; the lanes are used where
+// there is parallel work:
+//   * tables: the canonical code is built by the warp (histogram, ranks by __match_any_sync,
+//     one lookup entry per lane per step) into the warp's shared memory;
+//   * output: lane i holds the symbol for position i of the current 32-symbol group, so every
+//     group leaves in one 64-byte store, and long matches are written 256 symbols per
+//     instruction with 16-byte stores;
+//   * lookups: one 32-bit entry per code gives the literal, or a length/distance base with its
+//     extra-bit count, so a match costs two shared-memory reads.
+// A decoder whose extent fills takes a new one from the pool (an atomic on the pool's fill
+// level), so no decode needs a second launch; the extent records the exact decoder state where
+// it begins, so the host can cut a segment at any extent boundary.
+// Warps take jobs from a device queue (longest first), the grid is persistent: one wave of
+// blocks sized from the occupancy of this kernel.
+#include <cuda_runtime.h>
+
+#include "gi_common.cuh"
+
+namespace gz {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int NWARPS = 8;  // decoders per block
+constexpr int LB = 10;     // literal/length lookup bits
+constexpr int DB = 8;      // distance lookup bits
+constexpr int CB = 7;      // code-length code lookup bits (its codes are at most 7 bits)
+
+// lookup entry: bits 0-3 code length (0: longer than the lookup, or no code), 4-7 extra bits,
+// 8-23 value (literal byte, length base, distance base, code-length symbol), 24-25 kind
+constexpr uint32_t K_LIT = 0u << 24, K_LEN = 1u << 24, K_EOB = 2u << 24, K_BAD = 3u << 24;
+constexpr uint32_t E_LONG = K_BAD;  // kind BAD with code length 0: take the slow path
+
+struct Code {  // canonical code data for codes longer than the lookup
+    uint16_t first[16];  // first code of each length (MSB-first numbering)
+    uint16_t count[16];
+    uint16_t offs[16];   // index of the first symbol of each length in syms
+};
+
+struct __align__(16) Tables {
+    uint32_t lit[1 << LB];
+    uint32_t dist[1 << DB];
+    uint16_t lit_syms[288];
+    uint16_t dist_syms[32];
+    Code litc, distc, clc;
+    uint16_t cl_syms[19];
+    uint16_t running[16];
+    uint8_t lens[320];
+    uint8_t clh[1 << CB];  // (length << 5) | symbol
+    int32_t state;         // which tables are loaded: 0 none, 1 fixed, 2 dynamic
+    uint32_t pad;
+};
+
+__device__ const uint16_t c_lbase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                                         31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+__device__ const uint8_t c_lext[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+__device__ const uint16_t c_dbase[30] = {1,   2,   3,   4,   5,   7,    9,    13,   17,   25,   33,   49,    65,    97,    129,
+                                         193, 257, 385, 513, 769, 1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+__device__ const uint8_t c_dext[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+__device__ const uint8_t c_order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+
+enum Alphabet { A_LIT = 0, A_DIST = 1, A_CL = 2 };
+
+// the lookup entry of symbol s (without its code length)
+__device__ __forceinline__ uint32_t entry_of(int alphabet, int s) {
+    if (alphabet == A_LIT) {
+        if (s < 256) return K_LIT | ((uint32_t)s << 8);
+        if (s == 256) return K_EOB;
+        if (s < 286) return K_LEN | ((uint32_t)c_lbase[s - 257] << 8) | ((uint32_t)c_lext[s - 257] << 4);
+        return K_BAD;
+    }
+    if (alphabet == A_DIST) {
+        if (s < 30) return ((uint32_t)c_dbase[s] << 8) | ((uint32_t)c_dext[s] << 4);
+        return K_BAD;
+    }
+    return (uint32_t)s << 8;
+}
+
+struct Built {
+    int kraft;    // 0 complete, 1 incomplete, -1 over-subscribed
+    int nonzero;  // codes
+    int ones;     // codes of length 1
+};
+
+// Builds a canonical code from lens[0..n) (shared memory) with the whole warp: the lookup of
+// `root` bits (entries for codes up to root bits; E_LONG elsewhere), and Code/syms for longer
+// codes. The result is the same in every lane.
+__device__ Built build_code(const uint8_t* lens, int n, int alphabet, int root, uint32_t* lut, uint8_t* lut8, Code& c,
+                            uint16_t* syms, uint16_t* running, int lane) {
+    // histogram
+    if (lane < 16) c.count[lane] = 0;
+    __syncwarp();
+    for (int s0 = 0; s0 < n; s0 += 32) {
+        int s = s0 + lane;
+        int l = s < n ? lens[s] : -1;
+        unsigned peers = __match_any_sync(FULL, l);
+        int leader = __ffs(peers) - 1;
+        if (lane == leader && l >= 0) c.count[l] += (uint16_t)__popc(peers);
+        __syncwarp();
+    }
+    Built b;
+    b.nonzero = n - c.count[0];
+    b.ones = c.count[1];
+    int left = 1;
+    b.kraft = 0;
+    for (int len = 1; len < 16; len++) {
+        left = (left << 1) - c.count[len];
+        if (left < 0) {
+            b.kraft = -1;
+            break;
+        }
+    }
+    if (b.kraft < 0) return b;
+    b.kraft = left > 0 ? 1 : 0;
+    __syncwarp();
+    if (lane == 0) {
+        c.count[0] = 0;
+        uint16_t off = 0, code = 0;
+        for (int len = 1; len < 16; len++) {
+            code = (uint16_t)((code + (len > 1 ? c.count[len - 1] : 0)) << 1);
+            if (len == 1) code = 0;
+            c.first[len] = code;
+            c.offs[len] = off;
+            off = (uint16_t)(off + c.count[len]);
+        }
+    }
+    if (lane < 16) running[lane] = 0;
+    __syncwarp();
+    // symbols in canonical order (length, then symbol)
+    for (int s0 = 0; s0 < n; s0 += 32) {
+        int s = s0 + lane;
+        int l = s < n ? lens[s] : 0;
+        unsigned peers = __match_any_sync(FULL, l);
+        int rank = __popc(peers & ((1u << lane) - 1));
+        if (l) syms[c.offs[l] + running[l] + rank] = (uint16_t)s;
+        __syncwarp();
+        if (l && lane == 31 - __clz(peers)) running[l] += (uint16_t)__popc(peers);
+        __syncwarp();
+    }
+    // lookup entries: every (code of length <= root, filler bits) pair
+    const int size = 1 << root;
+    if (lut8) {
+        for (int i = lane; i < size; i += 32) lut8[i] = 0;
+    } else {
+        for (int i = lane; i < size; i += 32) lut[i] = E_LONG;
+    }
+    __syncwarp();
+    int ebase[16];
+    int e_total = 0;
+#pragma unroll
+    for (int len = 1; len < 16; len++) {
+        ebase[len] = e_total;
+        if (len <= root) e_total += c.count[len] << (root - len);
+    }
+    for (int e = lane; e < e_total; e += 32) {
+        int len = 1;
+        while (len < root && e >= ebase[len + 1]) len++;
+        int rel = e - ebase[len];
+        int r = rel >> (root - len);
+        int fill = rel & ((1 << (root - len)) - 1);
+        uint32_t j = ((uint32_t)(c.first[len] + r) << (root - len)) | (uint32_t)fill;  // MSB-first
+        uint32_t idx = __brev(j) >> (32 - root);                                        // stream order
+        int sym = syms[c.offs[len] + r];
+        if (lut8)
+            lut8[idx] = (uint8_t)((len << 5) | sym);
+        else
+            lut[idx] = entry_of(alphabet, sym) | (uint32_t)len;
+    }
+    __syncwarp();
+    return b;
+}
+
+struct Ctx {
+    DecodeArgs a;
+    Tables* T;
+    int lane;
+};
+
+// Bit reader, identical in every lane
+struct Bits {
+    const uint32_t* w;
+    uint64_t end_word;
+    uint64_t next;  // next word to load
+    uint64_t buf;
+    int cnt;
+
+    __device__ __forceinline__ void refill1() {
+        uint32_t v = next < end_word ? __ldg(w + next) : 0u;
+        buf |= (uint64_t)v << cnt;
+        next++;
+        cnt += 32;
+    }
+    __device__ __forceinline__ void init(const uint8_t* in, uint64_t endw, uint64_t bit) {
+        w = (const uint32_t*)in;
+        end_word = endw;
+        next = bit >> 5;
+        buf = 0;
+        cnt = 0;
+        refill1();
+        refill1();
+        int s = (int)(bit & 31);
+        buf >>= s;
+        cnt -= s;
+    }
+    __device__ __forceinline__ void need(int n) {
+        if (cnt < n) refill1();
+    }
+    __device__ __forceinline__ uint32_t get(int n) {  // n <= 32
+        need(n);
+        uint32_t v = (uint32_t)(buf & ((1ull << n) - 1));
+        buf >>= n;
+        cnt -= n;
+        return v;
+    }
+    __device__ __forceinline__ uint64_t pos() const { return next * 32 - (uint64_t)cnt; }
+};
+
+// symbol of a code longer than the lookup (or -1 entry)
+__device__ __forceinline__ uint32_t slow_decode(const Code& c, const uint16_t* syms, int alphabet, uint64_t buf,
+                                                int root) {
+    uint32_t rev = __brev((uint32_t)buf);
+    for (int len = root + 1; len < 16; len++) {
+        uint32_t code = rev >> (32 - len);
+        uint32_t d = code - c.first[len];
+        if (d < c.count[len]) return entry_of(alphabet, syms[c.offs[len] + d]) | (uint32_t)len;
+    }
+    return 0;  // no code: invalid data
+}
+
+// Reads a dynamic header's tables (after BFINAL/BTYPE). 0 ok, -1 invalid (inflate.cuh:231-265
+// and :393-402 state the rules).
+__device__ int dynamic_tables(Tables& T, Bits& br, int lane) {
+    T.state = 0;
+    int hlit = (int)br.get(5) + 257;
+    int hdist = (int)br.get(5) + 1;
+    int hclen = (int)br.get(4) + 4;
+    if (hlit > 286 || hdist > 30) return -1;
+    // the code-length code's lengths: read by every lane, each lane keeps one
+    uint32_t cl_bits = 0;
+    for (int i = 0; i < hclen; i++) {
+        uint32_t v = br.get(3);
+        if (lane < 19 && c_order[i] == lane) cl_bits = v;
+    }
+    if (lane < 19) T.lens[lane] = (uint8_t)cl_bits;
+    __syncwarp();
+    Built cb = build_code(T.lens, 19, A_CL, CB, nullptr, T.clh, T.clc, T.cl_syms, T.running, lane);
+    if (cb.kraft != 0) return -1;
+    int total = hlit + hdist;
+    int prev = 0;
+    for (int i = 0; i < total;) {
+        br.need(CB + 7);
+        uint32_t e = T.clh[br.buf & ((1u << CB) - 1)];
+        int len = (int)(e >> 5), sym = (int)(e & 31);
+        br.buf >>= len;
+        br.cnt -= len;
+        int rep = 1, val = sym;
+        if (sym >= 16) {
+            if (sym == 16) {
+                if (i == 0) return -1;
+                val = prev;
+                rep = 3 + (int)(br.buf & 3);
+                br.buf >>= 2;
+                br.cnt -= 2;
+            } else if (sym == 17) {
+                val = 0;
+                rep = 3 + (int)(br.buf & 7);
+                br.buf >>= 3;
+                br.cnt -= 3;
+            } else {
+                val = 0;
+                rep = 11 + (int)(br.buf & 127);
+                br.buf >>= 7;
+                br.cnt -= 7;
+            }
+            if (i + rep > total) return -1;
+        }
+        for (int k = lane; k < rep; k += 32) T.lens[i + k] = (uint8_t)val;
+        prev = val;
+        i += rep;
+    }
+    __syncwarp();
+    if (T.lens[256] == 0) return -1;
+    Built lb = build_code(T.lens, hlit, A_LIT, LB, T.lit, nullptr, T.litc, T.lit_syms, T.running, lane);
+    if (lb.kraft < 0 || (lb.kraft > 0 && !(lb.nonzero == 1 && lb.ones == 1))) return -1;
+    // distance lengths follow the literal/length ones
+    __syncwarp();
+    Built db = build_code(T.lens + hlit, hdist, A_DIST, DB, T.dist, nullptr, T.distc, T.dist_syms, T.running, lane);
+    if (db.kraft < 0 || (db.kraft > 0 && !(db.nonzero == 0 || (db.nonzero == 1 && db.ones == 1)))) return -1;
+    T.state = 2;
+    __syncwarp();
+    return 0;
+}
+
+__device__ void fixed_tables(Tables& T, int lane) {
+    if (T.state == 1) return;
+    __syncwarp();
+    for (int i = lane; i < 288; i += 32) T.lens[i] = (uint8_t)(i < 144 ? 8 : i < 256 ? 9 : i < 280 ? 7 : 8);
+    __syncwarp();
+    build_code(T.lens, 288, A_LIT, LB, T.lit, nullptr, T.litc, T.lit_syms, T.running, lane);
+    __syncwarp();
+    for (int i = lane; i < 30; i += 32) T.lens[i] = 5;
+    __syncwarp();
+    build_code(T.lens, 30, A_DIST, DB, T.dist, nullptr, T.distc, T.dist_syms, T.running, lane);
+    T.state = 1;
+    __syncwarp();
+}
+
+// the output side of a decoder: 32-symbol groups staged across the lanes
+struct Out {
+    uint16_t* base;   // current extent
+    uint64_t op;      // symbols in the current extent
+    uint64_t cap;
+    uint64_t done;    // symbols in earlier extents
+    int ext;          // current extent index
+    uint16_t stage;   // this lane's symbol of the current group
+};
+
+__device__ __forceinline__ void flush_partial(Out& o, int lane) {
+    uint32_t r = (uint32_t)(o.op & 31);
+    if (r && (uint32_t)lane < r) o.base[(o.op & ~31ull) + lane] = o.stage;
+}
+
+__device__ __forceinline__ void emit_lit(Out& o, uint32_t v, int lane) {
+    uint32_t r = (uint32_t)(o.op & 31);
+    if ((uint32_t)lane == r) o.stage = (uint16_t)v;
+    o.op++;
+    if (r == 31) o.base[o.op - 32 + lane] = o.stage;
+}
+
+__device__ __forceinline__ void emit_run(Out& o, uint32_t len, uint16_t v, int lane) {
+    uint32_t r = (uint32_t)(o.op & 31);
+    if ((uint32_t)lane - r < len) o.stage = v;
+    if (r + len < 32) {
+        o.op += len;
+        return;
+    }
+    uint64_t g = o.op & ~31ull;
+    o.base[g + lane] = o.stage;
+    uint64_t p = g + 32;
+    uint32_t rem = r + len - 32;
+    // 16-byte stores: 256 symbols per instruction (p is a multiple of 32: 64-byte aligned)
+    uint32_t w = (uint32_t)v | ((uint32_t)v << 16);
+    uint4 q = make_uint4(w, w, w, w);
+    uint32_t k = 0;
+    for (; k + 256 <= rem; k += 256) *(uint4*)(o.base + p + k + lane * 8) = q;
+    for (; k + 32 <= rem; k += 32) o.base[p + k + lane] = v;
+    o.stage = v;
+    o.op += len;
+}
+
+struct Job1 {
+    uint64_t stop;
+    uint64_t limit;     // min(stop, end_bit + 1): one comparison per symbol checks both
+    uint64_t end_bit;
+    uint64_t end_byte;
+    const Start* tg;
+    int t, tend;        // next target, end of the stream's targets
+    uint64_t tbit;      // targets[t].bit, or UINT64_MAX
+};
+
+// Starts a new extent for the decoder at `state`; false when the pool or the extent list is full.
+__device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, int job) {
+    int lane = C.lane;
+    flush_partial(o, lane);
+    uint64_t want = o.cap * 2;
+    if (want < (1ull << 20)) want = 1ull << 20;
+    if (want > (16ull << 20)) want = 16ull << 20;
+    if (want < need) want = (need + 31) & ~31ull;
+    unsigned long long off = 0;
+    int e = 0;
+    if (lane == 0) {
+        off = atomicAdd(&C.a.ctr->pool_used, (unsigned long long)want);
+        e = off + want <= C.a.pool_cap ? atomicAdd(&C.a.ctr->n_ext, 1) : -1;
+        if (e >= C.a.ext_cap) e = -1;
+    }
+    e = __shfl_sync(FULL, e, 0);
+    off = __shfl_sync(FULL, off, 0);
+    if (e < 0) return false;
+    if (lane == 0) {
+        C.a.ext[o.ext].len = o.op;
+        C.a.ext[o.ext].next = e;
+        Extent x;
+        x.pool_off = off;
+        x.len = 0;
+        x.cap = want;
+        x.start = state;
+        x.next = -1;
+        x.job = job;
+        C.a.ext[e] = x;
+    }
+    o.done += o.op;
+    o.op = 0;
+    o.cap = want;
+    o.base = C.a.pool + off;
+    o.ext = e;
+    return true;
+}
+
+__device__ void decode_job(Ctx& C, int k) {
+    const int lane = C.lane;
+    Tables& T = *C.T;
+    const Job J = C.a.jobs[k];
+    const StreamDesc S = C.a.streams[J.stream];
+    Job1 j;
+    j.stop = S.stop;
+    j.end_bit = S.end_bit;
+    j.end_byte = S.end_bit >> 3;
+    j.limit = S.stop < S.end_bit + 1 ? S.stop : S.end_bit + 1;
+    j.tg = C.a.targets;
+    j.t = J.tfirst;
+    j.tend = S.target_end;
+    j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
+    const bool check_refs = (J.flags & JOB_CHECK_REFS) != 0;
+
+    JobResult r;
+    r.eob_bit = UINT64_MAX;
+    r.eob_out = 0;
+    r.status = S_OK;
+    r.landed = -1;
+    r.end_final = J.start.mode == AT_BLOCK ? -1 : J.start.final;
+    r.blocks = 0;
+    r.resume = J.start;
+
+    Out o;
+    o.base = C.a.pool + J.pool_off;
+    o.op = 0;
+    o.cap = J.cap;
+    o.done = 0;
+    o.ext = k;
+    o.stage = 0;
+    if (lane == 0) {
+        Extent x;
+        x.pool_off = J.pool_off;
+        x.len = 0;
+        x.cap = J.cap;
+        x.start = J.start;
+        x.next = -1;
+        x.job = k;
+        C.a.ext[k] = x;
+    }
+
+    Bits br;
+    bool in_block = false, fixed = false;
+    uint64_t header = J.start.header;
+    if (J.start.mode == IN_FIXED) {
+        fixed_tables(T, lane);
+        in_block = fixed = true;
+    } else if (J.start.mode == IN_DYNAMIC) {
+        br.init(C.a.in, S.end_word, J.start.header);
+        br.get(3);
+        if (dynamic_tables(T, br, lane) != 0) {
+            r.status = S_DATA;
+            r.end_bit = J.start.bit;
+            r.out_len = 0;
+            if (lane == 0) C.a.res[k] = r;
+            return;
+        }
+        in_block = true;
+    }
+    br.init(C.a.in, S.end_word, J.start.bit);
+
+    for (;;) {
+        if (!in_block) {
+            uint64_t p = br.pos();
+            while (j.tbit < p) {
+                j.t++;
+                j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
+            }
+            if (j.tbit == p && j.tg[j.t].mode == AT_BLOCK) {
+                r.landed = j.t;
+                break;
+            }
+            if (p >= j.stop) {
+                r.status = S_STOPPED;
+                r.resume = Start{p, p, AT_BLOCK, -1, {0, 0, 0, 0, 0, 0}};
+                break;
+            }
+            if (o.op + MAX_SYMBOL_OUT > o.cap) {
+                Start st = Start{p, p, AT_BLOCK, -1, {0, 0, 0, 0, 0, 0}};
+                if (!new_extent(C, o, MAX_SYMBOL_OUT, st, k)) {
+                    r.status = S_OVERFLOW;
+                    r.resume = st;
+                    break;
+                }
+            }
+            if (p >= j.end_bit) {
+                r.status = S_INPUT;
+                break;
+            }
+            header = p;
+            int fin = (int)br.get(1);
+            int type = (int)br.get(2);
+            r.blocks++;
+            r.end_final = fin;
+            if (type == 0) {
+                uint32_t rb = (uint32_t)(br.pos() & 7);
+                if (rb) br.get(8 - (int)rb);
+                uint32_t len = br.get(16), nlen = br.get(16);
+                if (len != (~nlen & 0xffffu)) {
+                    r.status = S_DATA;
+                    break;
+                }
+                uint64_t byte = br.pos() >> 3;
+                if (byte + len > j.end_byte) {
+                    r.status = S_INPUT;
+                    break;
+                }
+                if (o.op + len > o.cap) {
+                    Start st = Start{p, p, AT_BLOCK, -1, {0, 0, 0, 0, 0, 0}};
+                    if (!new_extent(C, o, len + MAX_SYMBOL_OUT, st, k)) {
+                        r.status = S_OVERFLOW;
+                        r.resume = st;
+                        break;
+                    }
+                }
+                if (len) {
+                    flush_partial(o, lane);
+                    bool queued = false;
+                    if (lane == 0) {
+                        int i = atomicAdd(&C.a.ctr->n_stored, 1);
+                        if (i < C.a.stored_cap) {
+                            StoredCopy sc;
+                            sc.src = byte;
+                            sc.dst = (uint64_t)(o.base - C.a.pool) + o.op;
+                            sc.len = len;
+                            sc.pad = 0;
+                            C.a.stored[i] = sc;
+                            queued = true;
+                        }
+                    }
+                    queued = __shfl_sync(FULL, queued, 0);
+                    if (!queued) {  // list full: the warp copies the bytes itself
+                        for (uint32_t q = lane; q < len; q += 32) o.base[o.op + q] = C.a.in[byte + q];
+                        __syncwarp();
+                    }
+                    o.op += len;
+                    // the group the block ends in: its staged symbols must not overwrite its bytes
+                    if (!queued && (uint32_t)lane < (uint32_t)(o.op & 31)) o.stage = o.base[(o.op & ~31ull) + lane];
+                }
+                br.init(C.a.in, S.end_word, (byte + len) * 8);
+                if (fin) break;
+                continue;
+            }
+            if (type == 3) {
+                r.status = S_DATA;
+                break;
+            }
+            if (type == 1) {
+                fixed_tables(T, lane);
+                fixed = true;
+            } else {
+                if (dynamic_tables(T, br, lane) != 0) {
+                    r.status = S_DATA;
+                    break;
+                }
+                fixed = false;
+            }
+            in_block = true;
+        }
+        // ---- the block's symbols
+        const uint8_t mode = fixed ? IN_FIXED : IN_DYNAMIC;
+        bool eob = false;
+        for (;;) {
+            uint64_t p = br.pos();
+            if (p >= j.limit) {
+                if (p > j.end_bit) {
+                    r.status = S_INPUT;
+                } else {
+                    r.status = S_STOPPED;
+                    r.resume = Start{p, header, mode, (int8_t)r.end_final, {0, 0, 0, 0, 0, 0}};
+                }
+                break;
+            }
+            if (o.op + MAX_SYMBOL_OUT > o.cap) {
+                Start st = Start{p, header, mode, (int8_t)r.end_final, {0, 0, 0, 0, 0, 0}};
+                if (!new_extent(C, o, MAX_SYMBOL_OUT, st, k)) {
+                    r.status = S_OVERFLOW;
+                    r.resume = st;
+                    break;
+                }
+            }
+            br.need(32);
+            uint32_t e = T.lit[br.buf & ((1u << LB) - 1)];
+            if (e < (1u << 24)) {  // literal
+                int n = (int)(e & 15);
+                br.buf >>= n;
+                br.cnt -= n;
+                emit_lit(o, (e >> 8) & 255, lane);
+                continue;
+            }
+            if ((e & 15) == 0) {
+                e = slow_decode(T.litc, T.lit_syms, A_LIT, br.buf, LB);
+                if (e == 0) {
+                    r.status = S_DATA;
+                    break;
+                }
+                if (e < (1u << 24)) {
+                    int n = (int)(e & 15);
+                    br.buf >>= n;
+                    br.cnt -= n;
+                    emit_lit(o, (e >> 8) & 255, lane);
+                    continue;
+                }
+            }
+            uint32_t kind = e & (3u << 24);
+            if (kind == K_EOB) {
+                int n = (int)(e & 15);
+                br.buf >>= n;
+                br.cnt -= n;
+                eob = true;
+                break;
+            }
+            if (kind == K_BAD) {
+                r.status = S_DATA;
+                break;
+            }
+            // length
+            int n = (int)(e & 15), x = (int)((e >> 4) & 15);
+            uint32_t len = ((e >> 8) & 0xffff) + (uint32_t)((br.buf >> n) & ((1u << x) - 1));
+            br.buf >>= n + x;
+            br.cnt -= n + x;
+            br.need(32);
+            uint32_t de = T.dist[br.buf & ((1u << DB) - 1)];
+            if ((de & 15) == 0) {
+                de = de == E_LONG ? slow_decode(T.distc, T.dist_syms, A_DIST, br.buf, DB) : 0;
+                if (de == 0) {
+                    r.status = S_DATA;
+                    break;
+                }
+            }
+            if ((de & (3u << 24)) == K_BAD) {
+                r.status = S_DATA;
+                break;
+            }
+            int dn = (int)(de & 15), dx = (int)((de >> 4) & 15);
+            uint32_t d = ((de >> 8) & 0xffff) + (uint32_t)((br.buf >> dn) & ((1u << dx) - 1));
+            br.buf >>= dn + dx;
+            br.cnt -= dn + dx;
+            if (check_refs && r.blocks <= FIRST_RUN_BLOCKS && d > o.done + o.op) {
+                r.status = S_DATA;
+                break;
+            }
+            emit_run(o, len, (uint16_t)(REF + d), lane);
+        }
+        if (!eob) break;
+        in_block = false;
+        if (br.pos() > j.end_bit) {
+            r.status = S_INPUT;
+            break;
+        }
+        if (r.eob_bit == UINT64_MAX) {
+            r.eob_bit = br.pos();
+            r.eob_out = o.done + o.op;
+        }
+        if (r.end_final == 1) break;
+    }
+    flush_partial(o, lane);
+    r.end_bit = br.pos();
+    r.out_len = o.done + o.op;
+    if (lane == 0) {
+        C.a.ext[o.ext].len = o.op;
+        C.a.res[k] = r;
+    }
+}
+
+__global__ void __launch_bounds__(NWARPS * 32, 4) k_decode(DecodeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tables* tabs = (Tables*)smem;
+    Ctx C;
+    C.a = a;
+    C.lane = threadIdx.x & 31;
+    C.T = &tabs[threadIdx.x >> 5];
+    if (C.lane == 0) C.T->state = 0;
+    __syncwarp();
+    for (;;) {
+        int q = 0;
+        if (C.lane == 0) q = atomicAdd(&a.ctr->next_job, 1);
+        q = __shfl_sync(FULL, q, 0);
+        if (q >= a.njobs) break;
+        int k = a.order ? a.order[q] : q;
+        decode_job(C, k);
+    }
+}
+
+}  // namespace
+
+int decode_blocks_per_sm() {
+    int n = 0;
+    cudaFuncSetAttribute(k_decode, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(NWARPS * sizeof(Tables)));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_decode, NWARPS * 32, NWARPS * sizeof(Tables));
+    return n > 0 ? n : 1;
+}
+
+void launch_decode(const DecodeArgs& a, int grid, void* stream) {
+    k_decode<<<grid, NWARPS * 32, NWARPS * sizeof(Tables), (cudaStream_t)stream>>>(a);
+}
+
+}  // namespace gz

@@ -1,0 +1,258 @@
+// gi_find.cu - the block-start finder: for every chunk of the compressed input, the first bit
+// position that passes every check zlib applies to a dynamic-Huffman block header.
+//
+// The two tests are the reference's (gpuinflate/inflate.cuh:300-332): a cheap one on the 128
+// bits at a candidate (BTYPE 2, HLIT and HDIST at most 29, a complete code-length code) and the
+// full header check (code lengths decode, 16 not first, no repeat past the end, an end-of-block
+// code, Kraft rules for the literal/length and distance codes, and no read past the input).
+// The layout of the work is this file's own: a warp owns a chunk and walks it 32 words at a
+// time; each lane computes the BTYPE/HLIT/HDIST test for the 32 bit offsets of its word at once
+// as bit-sliced masks (a dozen shifts and ANDs instead of 32 tests), runs the code-length-code
+// test on the survivors, and the warp compacts the survivors in bit order through a ballot
+// prefix. Full checks then run 32 candidates at a time, one per lane, and the lowest passing
+// lane (a ballot) is the chunk's first start; the warp stops scanning the chunk there.
+#include <cuda_runtime.h>
+
+#include "gi_common.cuh"
+
+namespace gz {
+namespace {
+
+constexpr int FIND_WARPS = 8;
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t ldw(const uint32_t* w, uint64_t i, uint64_t end) {
+    return i < end ? __ldg(w + i) : 0u;
+}
+
+struct LaneBits {
+    const uint32_t* w;
+    uint64_t end_word;
+    uint64_t next;
+    uint64_t buf;
+    int cnt;
+
+    __device__ void init(const uint32_t* w_, uint64_t end_w, uint64_t bit) {
+        w = w_;
+        end_word = end_w;
+        next = bit >> 5;
+        buf = 0;
+        cnt = 0;
+        refill();
+        int s = (int)(bit & 31);
+        buf >>= s;
+        cnt -= s;
+    }
+    __device__ void refill() {
+        while (cnt <= 32) {
+            buf |= (uint64_t)ldw(w, next, end_word) << cnt;
+            next++;
+            cnt += 32;
+        }
+    }
+    __device__ uint32_t peek(int n) {
+        if (cnt < n) refill();
+        return (uint32_t)(buf & ((1ull << n) - 1));
+    }
+    __device__ void drop(int n) {
+        buf >>= n;
+        cnt -= n;
+    }
+    __device__ uint32_t get(int n) {
+        uint32_t v = peek(n);
+        drop(n);
+        return v;
+    }
+    __device__ uint64_t pos() const { return next * 32 - (uint64_t)cnt; }
+};
+
+__device__ const uint8_t c_cl_order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+
+// 0 complete, 1 incomplete, -1 over-subscribed, from counts per length (index 0 ignored)
+__device__ __forceinline__ int kraft_counts(const uint16_t* cnt) {
+    int left = 1;
+    for (int len = 1; len < 16; len++) {
+        left = (left << 1) - cnt[len];
+        if (left < 0) return -1;
+    }
+    return left > 0 ? 1 : 0;
+}
+
+// the full check of a dynamic header at `bit` (inflate.cuh:315-332 states the same rules)
+__device__ bool verify_header(const uint32_t* w, uint64_t end_word, uint64_t end_bit, uint64_t bit) {
+    LaneBits b;
+    b.init(w, end_word, bit);
+    b.drop(3);
+    int hlit = (int)b.get(5) + 257;
+    int hdist = (int)b.get(5) + 1;
+    int hclen = (int)b.get(4) + 4;
+    if (hlit > 286 || hdist > 30) return false;
+    uint8_t cl[19];
+    for (int i = 0; i < 19; i++) cl[i] = 0;
+    for (int i = 0; i < hclen; i++) cl[c_cl_order[i]] = (uint8_t)b.get(3);
+    uint16_t ccount[16];
+    for (int i = 0; i < 16; i++) ccount[i] = 0;
+    for (int i = 0; i < 19; i++) ccount[cl[i]]++;
+    ccount[0] = 0;
+    if (kraft_counts(ccount) != 0) return false;  // the code-length code must be complete
+    uint8_t sorted[19];
+    {
+        uint8_t offs[8];
+        offs[1] = 0;
+        for (int l = 1; l < 7; l++) offs[l + 1] = (uint8_t)(offs[l] + ccount[l]);
+        for (int s = 0; s < 19; s++)
+            if (cl[s]) sorted[offs[cl[s]]++] = (uint8_t)s;
+    }
+    uint16_t lit_cnt[16], dist_cnt[16];
+    for (int i = 0; i < 16; i++) lit_cnt[i] = dist_cnt[i] = 0;
+    int total = hlit + hdist;
+    int prev = 0;
+    bool eob = false;
+    for (int i = 0; i < total;) {
+        uint32_t bits = b.peek(7);
+        int code = 0, first = 0, index = 0, sym = -1;
+        for (int len = 1; len <= 7; len++) {
+            code |= (int)((bits >> (len - 1)) & 1);
+            int c = ccount[len];
+            if (code - c < first) {
+                b.drop(len);
+                sym = sorted[index + (code - first)];
+                break;
+            }
+            index += c;
+            first = (first + c) << 1;
+            code <<= 1;
+        }
+        if (sym < 0) return false;
+        int rep = 1, val = sym;
+        if (sym == 16) {
+            if (i == 0) return false;
+            val = prev;
+            rep = 3 + (int)b.get(2);
+        } else if (sym == 17) {
+            val = 0;
+            rep = 3 + (int)b.get(3);
+        } else if (sym == 18) {
+            val = 0;
+            rep = 11 + (int)b.get(7);
+        }
+        if (i + rep > total) return false;
+        // counts per length for the two codes; position 256 is the end-of-block code
+        int nlit = i < hlit ? min(rep, hlit - i) : 0;
+        lit_cnt[val] += (uint16_t)nlit;
+        dist_cnt[val] += (uint16_t)(rep - nlit);
+        if (i <= 256 && 256 < i + rep && 256 < hlit) eob = val != 0;
+        prev = val;
+        i += rep;
+    }
+    if (!eob) return false;
+    int nz = hlit - lit_cnt[0], ones = lit_cnt[1];
+    int r = kraft_counts(lit_cnt);
+    if (r < 0 || (r > 0 && !(nz == 1 && ones == 1))) return false;
+    nz = hdist - dist_cnt[0];
+    ones = dist_cnt[1];
+    r = kraft_counts(dist_cnt);
+    if (r < 0 || (r > 0 && !(nz == 0 || (nz == 1 && ones == 1)))) return false;
+    return b.pos() <= end_bit;
+}
+
+// code-length code complete, from the 128 bits at a candidate whose first 17 bits passed
+__device__ __forceinline__ bool cl_code_complete(uint64_t v1, uint64_t v2) {
+    int hclen = (int)((v1 >> 13) & 15) + 4;
+    uint64_t f = (v1 >> 17) | (v2 << 47);
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+        uint32_t l = (uint32_t)(f >> (3 * i)) & 7;
+        uint32_t add = (uint32_t)(0x0102040810204000ull >> (8 * l)) & 0xff;  // 128 >> l, 0 for l = 0
+        sum += i < hclen ? add : 0;
+    }
+    return sum == 128;
+}
+
+__global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __restrict__ w, uint64_t bit_lo,
+                                                          uint64_t bit_hi, uint64_t end_word, uint64_t end_bit,
+                                                          uint32_t chunk_bits, uint64_t nchunks,
+                                                          uint64_t* __restrict__ first) {
+    __shared__ uint16_t cand[FIND_WARPS][1024];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint64_t nwarps = (uint64_t)gridDim.x * FIND_WARPS;
+    for (uint64_t c = (uint64_t)blockIdx.x * FIND_WARPS + wib; c < nchunks; c += nwarps) {
+        uint64_t cb = bit_lo + c * chunk_bits;
+        uint64_t lo = cb > bit_lo ? cb : bit_lo + 1;  // candidates are strictly after bit_lo
+        uint64_t hi = cb + chunk_bits < bit_hi ? cb + chunk_bits : bit_hi;
+        uint64_t found = UINT64_MAX;
+        if (lo < hi) {
+            uint64_t w0 = lo >> 5, w1 = (hi + 31) >> 5;
+            for (uint64_t ws = w0; ws < w1 && found == UINT64_MAX; ws += 32) {
+                uint64_t wi = ws + lane;
+                uint32_t mask = 0;
+                if (wi < w1) {
+                    uint64_t a = ldw(w, wi, end_word), b = ldw(w, wi + 1, end_word);
+                    uint64_t c2 = ldw(w, wi + 2, end_word), d = ldw(w, wi + 3, end_word);
+                    uint64_t lo64 = a | b << 32, hi64 = c2 | d << 32;
+                    // bit-sliced: bit o of m is the test for the offset wi*32+o
+                    uint64_t m = ~(lo64 >> 1) & (lo64 >> 2);                          // BTYPE = 2
+                    m &= ~((lo64 >> 4) & (lo64 >> 5) & (lo64 >> 6) & (lo64 >> 7));    // HLIT <= 29
+                    m &= ~((lo64 >> 9) & (lo64 >> 10) & (lo64 >> 11) & (lo64 >> 12)); // HDIST <= 29
+                    mask = (uint32_t)m;
+                    uint64_t base = wi * 32;
+                    if (base < lo) mask &= ~0u << (uint32_t)(lo - base);
+                    if (base + 32 > hi) mask &= (1u << (uint32_t)(hi - base)) - 1;
+                    uint32_t keep = 0, mm = mask;
+                    while (mm) {
+                        int o = __ffs(mm) - 1;
+                        mm &= mm - 1;
+                        uint64_t v1 = o ? (lo64 >> o) | (hi64 << (64 - o)) : lo64;
+                        uint64_t v2 = hi64 >> o;
+                        if (cl_code_complete(v1, v2)) keep |= 1u << o;
+                    }
+                    mask = keep;
+                }
+                // survivors, in bit order, into the warp's list
+                int n = __popc(mask), incl = n;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    int v = __shfl_up_sync(FULL, incl, d);
+                    if (lane >= d) incl += v;
+                }
+                int total = __shfl_sync(FULL, incl, 31);
+                int j = incl - n;
+                for (uint32_t mm = mask; mm; mm &= mm - 1) cand[wib][j++] = (uint16_t)((lane << 5) | (__ffs(mm) - 1));
+                __syncwarp();
+                for (int b0 = 0; b0 < total; b0 += 32) {
+                    bool ok = false;
+                    uint64_t bit = 0;
+                    if (b0 + lane < total) {
+                        uint32_t e = cand[wib][b0 + lane];
+                        bit = (ws + (e >> 5)) * 32 + (e & 31);
+                        ok = verify_header(w, end_word, end_bit, bit);
+                    }
+                    uint32_t bal = __ballot_sync(FULL, ok);
+                    if (bal) {
+                        found = __shfl_sync(FULL, bit, __ffs(bal) - 1);
+                        break;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (lane == 0) first[c] = found;
+    }
+}
+
+}  // namespace
+
+void launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
+                 uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, void* stream) {
+    if (!nchunks) return;
+    int dev = 0, nsm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    uint64_t blocks = (nchunks + FIND_WARPS - 1) / FIND_WARPS;
+    uint64_t cap = (uint64_t)nsm * 8;
+    k_find<<<(unsigned)(blocks < cap ? blocks : cap), FIND_WARPS * 32, 0, (cudaStream_t)stream>>>(
+        (const uint32_t*)d_in, bit_lo, bit_hi, end_word, end_bit, chunk_bits, nchunks, d_first);
+}
+
+}  // namespace gz

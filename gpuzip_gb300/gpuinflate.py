@@ -1,0 +1,201 @@
+"""Python binding of libgpuinflate.so over its C interface (ctypes).
+
+It calls the library the way gpuzip's Rust host does (src/inflate.rs:110-168): load the shared
+library, check ``gi_abi_version() == 1``, create one context with ``gi_config{16, device, 0, 0}``
+and a 512-byte error buffer, serialise calls on a lock (a context serves one call at a time),
+pass a sink callback that returns nonzero to stop, and map the return codes 1/2/3/other to
+data / truncated / aborted / GPU errors. There is no CPU fallback: without the built library or
+a GPU every call raises.
+"""
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgpuinflate.so")
+ABI_VERSION = 1
+
+GI_OK, GI_ERR_DATA, GI_ERR_TRUNCATED, GI_ERR_ABORTED, GI_ERR_GPU, GI_ERR_ARG, GI_ERR_SPACE = range(7)
+
+EXPORTED = (
+    "gi_abi_version",
+    "gi_create",
+    "gi_inflate",
+    "gi_last_error",
+    "gi_device_name",
+    "gi_destroy",
+    "gi_last_crc32",
+    "gi_last_isize",
+    "gi_inflate_device",
+    "gi_inflate_gzip",
+)
+
+
+class Config(ctypes.Structure):
+    """gi_config (gpuinflate.h)"""
+
+    _fields_ = [("size", ctypes.c_uint32), ("device", ctypes.c_int32), ("segment_out_mb", ctypes.c_uint32),
+                ("segment_in_kb", ctypes.c_uint32)]
+
+
+class Stats(ctypes.Structure):
+    """gi_stats (gpuinflate.h)"""
+
+    _fields_ = [("in_used", ctypes.c_uint64), ("out_size", ctypes.c_uint64), ("segments", ctypes.c_uint32),
+                ("rounds", ctypes.c_uint32), ("jobs", ctypes.c_uint64), ("seconds", ctypes.c_double),
+                ("upload_s", ctypes.c_double), ("find_s", ctypes.c_double), ("decode_s", ctypes.c_double),
+                ("resolve_s", ctypes.c_double), ("download_s", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t)
+
+
+class InflateError(Exception):
+    def __init__(self, code, msg):
+        super().__init__(f"{['ok', 'data', 'truncated', 'aborted', 'gpu', 'arg', 'space'][code] if code < 7 else code}: {msg}")
+        self.code = code
+        self.msg = msg
+
+
+_lib = None
+
+
+def load(path=None):
+    """The library, loaded once; raises when it is missing or speaks another interface version."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is not built (run gpuzip_gb300/build.py)")
+    lib = ctypes.CDLL(path)
+    lib.gi_abi_version.restype = ctypes.c_uint32
+    if lib.gi_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{path} speaks interface {lib.gi_abi_version()}, expected {ABI_VERSION}")
+    vp, u64 = ctypes.c_void_p, ctypes.c_uint64
+    lib.gi_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t]
+    lib.gi_create.restype = ctypes.c_int
+    lib.gi_inflate.argtypes = [vp, ctypes.c_char_p, u64, u64, SINK, vp, ctypes.POINTER(Stats)]
+    lib.gi_inflate.restype = ctypes.c_int
+    lib.gi_last_error.argtypes = [vp]
+    lib.gi_last_error.restype = ctypes.c_char_p
+    lib.gi_device_name.argtypes = [vp]
+    lib.gi_device_name.restype = ctypes.c_char_p
+    lib.gi_destroy.argtypes = [vp]
+    lib.gi_destroy.restype = None
+    lib.gi_last_crc32.argtypes = [vp]
+    lib.gi_last_crc32.restype = ctypes.c_uint32
+    lib.gi_last_isize.argtypes = [vp]
+    lib.gi_last_isize.restype = ctypes.c_uint32
+    lib.gi_inflate_device.argtypes = [vp, vp, u64, vp, u64, ctypes.POINTER(u64), ctypes.POINTER(Stats)]
+    lib.gi_inflate_device.restype = ctypes.c_int
+    lib.gi_inflate_gzip.argtypes = [vp, ctypes.c_char_p, u64, SINK, vp, ctypes.POINTER(u64), ctypes.POINTER(Stats)]
+    lib.gi_inflate_gzip.restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+class Gpu:
+    """One decoding context on one GPU (the Rust host's inflate::Gpu)."""
+
+    def __init__(self, device=0, segment_out_mb=0, segment_in_kb=0, path=None):
+        self.lib = load(path)
+        cfg = Config(ctypes.sizeof(Config), device, segment_out_mb, segment_in_kb)
+        ctx = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(512)
+        rc = self.lib.gi_create(ctypes.byref(cfg), ctypes.byref(ctx), err, 512)
+        if rc != GI_OK:
+            raise InflateError(rc, f"GPU not usable: {err.value.decode(errors='replace')}")
+        self.ctx = ctx
+        self.device = self.lib.gi_device_name(ctx).decode(errors="replace")
+        self._lock = threading.Lock()
+
+    def close(self):
+        if self.ctx:
+            self.lib.gi_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _error(self, rc):
+        return InflateError(rc, self.lib.gi_last_error(self.ctx).decode(errors="replace"))
+
+    def inflate(self, data, hint=0, sink=None, collect=True):
+        """Decodes the raw Deflate stream at the start of `data`. Returns (output bytes or None,
+        Stats). sink(chunk) -> bool (False stops) receives the output when given."""
+        parts = []
+
+        def _cb(user, ptr, n):
+            try:
+                chunk = ctypes.string_at(ptr, n)
+                if sink is not None:
+                    return 0 if sink(chunk) else 1
+                parts.append(chunk)
+                return 0
+            except Exception:
+                return 1
+
+        cb = SINK(_cb) if (sink is not None or collect) else SINK()
+        st = Stats()
+        buf = bytes(data)
+        with self._lock:
+            rc = self.lib.gi_inflate(self.ctx, buf, len(buf), hint, cb, None, ctypes.byref(st))
+            if rc != GI_OK:
+                raise self._error(rc)
+        return (b"".join(parts) if collect and sink is None else None), st
+
+    def inflate_status(self, data, hint=0):
+        """(return code, output, in_used) without raising on data errors (for parity tests)."""
+        parts = []
+
+        def _cb(user, ptr, n):
+            parts.append(ctypes.string_at(ptr, n))
+            return 0
+
+        st = Stats()
+        buf = bytes(data)
+        with self._lock:
+            rc = self.lib.gi_inflate(self.ctx, buf, len(buf), hint, SINK(_cb), None, ctypes.byref(st))
+        return rc, (b"".join(parts) if rc == GI_OK else b""), st.in_used
+
+    def inflate_gzip(self, member):
+        """Decodes one gzip member with the CRC-32/ISIZE check done on the GPU. Returns (output,
+        member size, Stats)."""
+        parts = []
+
+        def _cb(user, ptr, n):
+            parts.append(ctypes.string_at(ptr, n))
+            return 0
+
+        st = Stats()
+        msize = ctypes.c_uint64(0)
+        buf = bytes(member)
+        with self._lock:
+            rc = self.lib.gi_inflate_gzip(self.ctx, buf, len(buf), SINK(_cb), None, ctypes.byref(msize), ctypes.byref(st))
+            if rc != GI_OK:
+                raise self._error(rc)
+        return b"".join(parts), msize.value, st
+
+    def inflate_device(self, d_in, in_size, d_out, out_cap):
+        """Device-resident form: pointers (ints) to GPU memory. Returns (out_size, Stats)."""
+        st = Stats()
+        n = ctypes.c_uint64(0)
+        with self._lock:
+            rc = self.lib.gi_inflate_device(self.ctx, ctypes.c_void_p(d_in), in_size, ctypes.c_void_p(d_out), out_cap,
+                                            ctypes.byref(n), ctypes.byref(st))
+            if rc != GI_OK:
+                raise self._error(rc)
+        return n.value, st
+
+    def last_crc32(self):
+        return self.lib.gi_last_crc32(self.ctx)
+
+    def last_isize(self):
+        return self.lib.gi_last_isize(self.ctx)

@@ -1,0 +1,313 @@
+"""Seeded synthetic Deflate workloads (the inputs the decoder is tested and measured on).
+
+None of the reference's datasets are reproduced: every stream here is generated from a seed.
+
+* ``log_text`` - log lines ``YYYY-MM-DD HH:MM:SS LEVEL w1 w2 ... wn\\n`` with 5-25 words drawn
+  Zipf(s=1.1) (rank r has weight r**-1.1) from a 10,000-word vocabulary of 3-12 random lowercase
+  letters; LEVEL uniform over INFO/WARN/ERROR/DEBUG; the timestamp advances 0-3 s per line.
+* ``single_text_member`` - 64 MiB of that text (cut at the end of the line that crosses 64 MiB)
+  as one gzip member, zlib level 6, 32 KiB window.
+* ``mixed_member`` - one gzip member of ``nseg`` segments of 1 MiB each, every segment one of:
+  log text (p=0.50), uniform random bytes (0.20), a 4-64-byte pattern repeated with 1% of its
+  bytes replaced at random (0.15), little-endian uint32 counters with small random deltas
+  (0.15); each segment compressed at a level drawn from {1, 6, 9}, all inside ONE Deflate
+  stream: every segment is compressed with the previous 32 KiB of output as its preset
+  dictionary and ended with a sync flush, so matches reach across segments and the segments
+  join into one stream (the last one carries the final block). 4096 segments = 4 GiB, whose
+  gzip ISIZE wraps to 0.
+* ``fuzz_streams`` - eight small raw streams of every block kind (levels 1/6/9, fixed only,
+  stored only, Huffman only, mixed random/text/runs, tiny), the kinds the reference fuzzes
+  (gpuinflate/make_fuzz_inputs.py); made from this module's own text.
+"""
+import multiprocessing as mp
+import struct
+import zlib
+
+import numpy as np
+
+MIB = 1 << 20
+LEVELS = (b"INFO", b"WARN", b"ERROR", b"DEBUG")
+T0 = 1704067200  # 2024-01-01 00:00:00 UTC
+
+# ---------------------------------------------------------------- CRC-32 arithmetic
+
+POLY = 0xEDB88320
+
+
+def _mulmod(a, b):
+    """a(x) * b(x) mod the CRC polynomial, in the reflected bit order CRC-32 uses (bit 31 = x^0)."""
+    p = 0
+    m = 1 << 31
+    while m:
+        if a & m:
+            p ^= b
+        b = (b >> 1) ^ POLY if b & 1 else b >> 1
+        m >>= 1
+    return p
+
+
+_X2N = []
+_p = 1 << 30  # x^1
+for _ in range(64):
+    _X2N.append(_p)
+    _p = _mulmod(_p, _p)
+
+
+def _x8n(n):
+    """x^(8n) mod P"""
+    p = 1 << 31
+    k = 3
+    while n:
+        if n & 1:
+            p = _mulmod(_X2N[k % 64], p)
+        n >>= 1
+        k += 1
+    return p
+
+
+def crc32_combine(crc1, crc2, len2):
+    """CRC-32 of A+B from crc(A), crc(B) and len(B)."""
+    return _mulmod(_x8n(len2), crc1) ^ crc2
+
+
+# ---------------------------------------------------------------- log text
+
+
+class _Vocab:
+    def __init__(self, seed):
+        rng = np.random.default_rng([seed, 7_000_001])
+        self.lens = rng.integers(3, 13, size=10000)
+        self.chars = rng.integers(97, 123, size=int(self.lens.sum()), dtype=np.uint8)
+        self.offs = np.concatenate([[0], np.cumsum(self.lens)[:-1]])
+        w = np.arange(1, 10001, dtype=np.float64) ** -1.1
+        c = np.cumsum(w)
+        self.cdf = c / c[-1]
+
+
+_VOCABS = {}
+
+
+def _vocab(seed):
+    if seed not in _VOCABS:
+        _VOCABS[seed] = _Vocab(seed)
+    return _VOCABS[seed]
+
+
+def _lines(rng, voc, nlines, t_start):
+    """nlines log lines as one uint8 array, and the next timestamp."""
+    nw = rng.integers(5, 26, size=nlines)
+    dt = rng.integers(0, 4, size=nlines)
+    t = t_start + np.cumsum(dt) - dt[0]
+    lev = rng.integers(0, 4, size=nlines)
+    ids = np.searchsorted(voc.cdf, rng.random(int(nw.sum())), side="right")
+    ids = np.minimum(ids, 9999)
+    wl = voc.lens[ids]
+    lev_len = np.array([len(x) for x in LEVELS])[lev]
+    hdr = 20 + lev_len + 1  # "YYYY-MM-DD HH:MM:SS " + LEVEL + " "
+    body = np.add.reduceat(wl + 1, np.concatenate([[0], np.cumsum(nw)[:-1]]))
+    line_len = hdr + body
+    ls = np.concatenate([[0], np.cumsum(line_len)[:-1]])
+    total = int(line_len.sum())
+    out = np.empty(total, dtype=np.uint8)
+    ts = np.datetime_as_string(t.astype("datetime64[s]")).astype("S19")
+    tsb = np.frombuffer(ts.tobytes(), dtype=np.uint8).reshape(nlines, 19).copy()
+    tsb[:, 10] = ord(" ")
+    out[ls[:, None] + np.arange(19)] = tsb
+    out[ls + 19] = ord(" ")
+    for k, name in enumerate(LEVELS):
+        sel = ls[lev == k]
+        if len(sel):
+            out[sel[:, None] + 20 + np.arange(len(name))] = np.frombuffer(name, dtype=np.uint8)
+            out[sel + 20 + len(name)] = ord(" ")
+    # words: position of each word in its line's body
+    line_of_word = np.repeat(np.arange(nlines), nw)
+    cw = np.concatenate([[0], np.cumsum(wl + 1)[:-1]])
+    first_word = np.concatenate([[0], np.cumsum(nw)[:-1]])
+    wpos = ls[line_of_word] + hdr[line_of_word] + (cw - cw[first_word][line_of_word])
+    nchar = int(wl.sum())
+    within = np.arange(nchar) - np.repeat(np.concatenate([[0], np.cumsum(wl)[:-1]]), wl)
+    out[np.repeat(wpos, wl) + within] = voc.chars[np.repeat(voc.offs[ids], wl) + within]
+    sep = np.full(len(ids), ord(" "), dtype=np.uint8)
+    sep[np.cumsum(nw) - 1] = ord("\n")
+    out[wpos + wl] = sep
+    return out, int(t[-1]) + int(rng.integers(0, 4))
+
+
+def log_text(seed, nbytes, exact=False, t_start=T0, vocab_seed=None):
+    """At least nbytes of log text, cut at the end of the line that crosses nbytes (or exactly
+    nbytes when exact)."""
+    voc = _vocab(seed if vocab_seed is None else vocab_seed)
+    rng = np.random.default_rng(seed)
+    parts, have, t = [], 0, t_start
+    while have < nbytes:
+        need = nbytes - have
+        n = max(64, min(200_000, need // 100 + 16))
+        arr, t = _lines(rng, voc, n, t)
+        parts.append(arr)
+        have += len(arr)
+    text = np.concatenate(parts)
+    if exact:
+        return text[:nbytes].tobytes()
+    end = int(np.argmax(text[nbytes - 1 :] == ord("\n"))) + nbytes if have > nbytes else have
+    return text[:end].tobytes()
+
+
+# ---------------------------------------------------------------- containers
+
+
+def gzip_wrap(deflated, crc, isize, mtime=0):
+    return b"\x1f\x8b\x08\x00" + struct.pack("<I", mtime) + b"\x00\xff" + deflated + struct.pack("<II", crc, isize & 0xFFFFFFFF)
+
+
+def raw_deflate(data, level=6, strategy=zlib.Z_DEFAULT_STRATEGY, zdict=None, final=True):
+    kw = {"zdict": zdict} if zdict else {}
+    c = zlib.compressobj(level, zlib.DEFLATED, -15, 9, strategy, **kw)
+    return c.compress(data) + c.flush(zlib.Z_FINISH if final else zlib.Z_SYNC_FLUSH)
+
+
+def single_text_member(seed=1, nbytes=64 * MIB):
+    """(gzip member, text): the single-member log-text workload."""
+    text = log_text(seed, nbytes)
+    body = raw_deflate(text, 6)
+    return gzip_wrap(body, zlib.crc32(text), len(text)), text
+
+
+# ---------------------------------------------------------------- mixed content
+
+KIND_TEXT, KIND_RANDOM, KIND_PATTERN, KIND_COUNTER = 0, 1, 2, 3
+
+
+def mixed_plan(seed, nseg):
+    """(kinds, levels) of every segment."""
+    rng = np.random.default_rng([seed, 1])
+    kinds = rng.choice(4, size=nseg, p=[0.5, 0.2, 0.15, 0.15])
+    levels = rng.choice(np.array([1, 6, 9]), size=nseg)
+    return kinds, levels
+
+
+def mixed_segment(seed, index, kind, seg_bytes=MIB):
+    """The content of segment `index` of the mixed workload (exactly seg_bytes)."""
+    rng = np.random.default_rng([seed, 2, index])
+    if kind == KIND_TEXT:
+        return log_text(int(rng.integers(1 << 62)), seg_bytes, exact=True, t_start=T0 + 3600 * index, vocab_seed=seed)
+    if kind == KIND_RANDOM:
+        return rng.integers(0, 256, size=seg_bytes, dtype=np.uint8).tobytes()
+    if kind == KIND_PATTERN:
+        p = int(rng.integers(4, 65))
+        pat = rng.integers(0, 256, size=p, dtype=np.uint8)
+        a = np.tile(pat, seg_bytes // p + 1)[:seg_bytes]
+        nflip = seg_bytes // 100
+        a[rng.integers(0, seg_bytes, size=nflip)] = rng.integers(0, 256, size=nflip, dtype=np.uint8)
+        return a.tobytes()
+    start = int(rng.integers(0, 1 << 32))
+    deltas = rng.integers(0, 16, size=seg_bytes // 4, dtype=np.uint64)
+    vals = (start + np.cumsum(deltas)) & 0xFFFFFFFF
+    return vals.astype("<u4").tobytes()
+
+
+def _mixed_job(args):
+    seed, index, nseg, kind, prev_kind, level, seg_bytes = args
+    data = mixed_segment(seed, index, kind, seg_bytes)
+    zdict = mixed_segment(seed, index - 1, prev_kind, seg_bytes)[-32768:] if index > 0 else None
+    body = raw_deflate(data, int(level), zdict=zdict, final=index == nseg - 1)
+    return index, body, zlib.crc32(data), len(data)
+
+
+def mixed_member(seed=2, nseg=4096, seg_bytes=MIB, workers=None, want_raw=False):
+    """(gzip member, info) of the mixed workload. info: crc, size, kinds, levels, deflate offset,
+    and the raw output when want_raw (only for small nseg)."""
+    kinds, levels = mixed_plan(seed, nseg)
+    jobs = [(seed, i, nseg, int(kinds[i]), int(kinds[i - 1]) if i else 0, int(levels[i]), seg_bytes) for i in range(nseg)]
+    workers = workers or min(mp.cpu_count(), 32)
+    if nseg >= 8 and workers > 1:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(workers) as pool:
+            res = pool.map(_mixed_job, jobs, chunksize=max(1, nseg // (workers * 8)))
+    else:
+        res = [_mixed_job(j) for j in jobs]
+    res.sort(key=lambda r: r[0])
+    crc, size = 0, 0
+    for _, _, c, n in res:
+        crc = crc32_combine(crc, c, n)
+        size += n
+    body = b"".join(r[1] for r in res)
+    member = gzip_wrap(body, crc, size)
+    info = {"crc": crc, "size": size, "kinds": kinds, "levels": levels, "deflate_offset": 10, "deflate_size": len(body)}
+    if want_raw:
+        info["raw"] = b"".join(mixed_segment(seed, i, int(kinds[i]), seg_bytes) for i in range(nseg))
+    return member, info
+
+
+# ---------------------------------------------------------------- fuzz inputs
+
+
+def fuzz_streams(seed=7):
+    """name -> raw Deflate stream, every block kind (small: for fuzzing and parity)."""
+    text = log_text(seed, 2 * MIB)
+    rng = np.random.default_rng(seed)
+    mixed = bytearray()
+    while len(mixed) < MIB:
+        k = int(rng.integers(3))
+        n = int(rng.integers(1, 40000))
+        if k == 0:
+            mixed += rng.integers(0, 256, size=n, dtype=np.uint8).tobytes()
+        elif k == 1:
+            a = int(rng.integers(len(text) - n))
+            mixed += text[a : a + n]
+        else:
+            mixed += bytes([int(rng.integers(256))]) * n
+    return {
+        "f-l1": raw_deflate(text[:MIB], 1),
+        "f-l6": raw_deflate(text, 6),
+        "f-l9": raw_deflate(text[:MIB], 9),
+        "f-fixed": raw_deflate(text[:MIB], 6, zlib.Z_FIXED),
+        "f-stored": raw_deflate(text[: 512 << 10], 0),
+        "f-mixed": raw_deflate(bytes(mixed), 6),
+        "f-huffman": raw_deflate(text[:MIB], 6, zlib.Z_HUFFMAN_ONLY),
+        "f-tiny": raw_deflate(b"hello, hello, hello world\n" * 3, 6),
+    }
+
+
+class SplitMix64:
+    """The mutation RNG of the reference's fuzzer (gpuinflate/gi_test.cpp:99-108)."""
+
+    def __init__(self, seed):
+        self.s = seed & 0xFFFFFFFFFFFFFFFF
+
+    def next(self):
+        M = 0xFFFFFFFFFFFFFFFF
+        self.s = (self.s + 0x9E3779B97F4A7C15) & M
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+        return z ^ (z >> 31)
+
+    def below(self, n):
+        return self.next() % n if n else 0
+
+
+def mutate(data, rng):
+    """One damaged copy of data: 1-4 of the reference fuzzer's six mutation kinds
+    (gpuinflate/gi_test.cpp:197-218): bit flip (twice as likely), byte overwrite, span of
+    1-64 random bytes, truncation, a copied span of up to 4096 bytes."""
+    m = bytearray(data)
+    for _ in range(1 + rng.below(4)):
+        if not m:
+            break
+        k = rng.below(6)
+        if k in (0, 1):
+            m[rng.below(len(m))] ^= 1 << rng.below(8)
+        elif k == 2:
+            m[rng.below(len(m))] = rng.next() & 0xFF
+        elif k == 3:
+            a = rng.below(len(m))
+            n = min(1 + rng.below(64), len(m) - a)
+            for i in range(n):
+                m[a + i] = rng.next() & 0xFF
+        elif k == 4:
+            del m[rng.below(len(m)) + 1 :]
+        else:
+            a, b = rng.below(len(m)), rng.below(len(m))
+            n = min(1 + rng.below(4096), len(m) - a, len(m) - b)
+            m[b : b + n] = m[a : a + n]
+    return bytes(m)

@@ -1,0 +1,122 @@
+/* gpuinflate.h - C interface of the GB300-native Deflate decoder (libgpuinflate.so).
+ *
+ * Part 1 is interface version 1 of gpuzip's gpuinflate library, kept symbol for symbol and
+ * byte for byte so that gpuzip's Rust host (src/inflate.rs) loads this library unchanged:
+ * the same names, the same argument meaning, the same return codes and the same struct
+ * layouts. Part 2 adds entry points that the reference does not have; adding symbols does not
+ * change version 1.
+ *
+ * One context serves one call at a time; use one context per host thread. */
+#ifndef GPUINFLATE_H
+#define GPUINFLATE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(GI_BUILD) && defined(__GNUC__)
+#define GI_API __attribute__((visibility("default")))
+#else
+#define GI_API
+#endif
+
+/* ------------------------------------------------------------------ part 1: interface 1 */
+
+/* reference: gpuinflate/gpuinflate.h:31 */
+#define GI_ABI_VERSION 1
+
+/* Return codes. reference: gpuinflate/gpuinflate.h:33-40 (same values) */
+enum {
+    GI_OK = 0,
+    GI_ERR_DATA = 1,      /* not a valid Deflate stream (a match reaching before the start included) */
+    GI_ERR_TRUNCATED = 2, /* the input stops before the stream's final block ends (or is empty) */
+    GI_ERR_ABORTED = 3,   /* the sink asked to stop */
+    GI_ERR_GPU = 4,       /* no usable GPU, GPU memory exhausted, or a CUDA failure */
+    GI_ERR_ARG = 5,       /* an invalid argument */
+    GI_ERR_SPACE = 6      /* part 2 only: the output does not fit the caller's buffer */
+};
+
+typedef struct gi_ctx gi_ctx;
+
+/* reference: gpuinflate/gpuinflate.h:44-49 (16 bytes; same fields, same order) */
+typedef struct {
+    uint32_t size;           /* sizeof(gi_config); smaller is an argument error */
+    int32_t device;          /* CUDA device ordinal */
+    uint32_t segment_out_mb; /* largest output of one segment in MiB; 0 picks it from free GPU memory */
+    uint32_t segment_in_kb;  /* compressed input per segment in KiB; 0 picks it from the stream's ratio */
+} gi_config;
+
+/* reference: gpuinflate/gpuinflate.h:51-59 (80 bytes; same fields, same order) */
+typedef struct {
+    uint64_t in_used;  /* input bytes the stream occupies, through its final block, rounded up to a byte */
+    uint64_t out_size; /* output bytes produced */
+    uint32_t segments; /* segments the stream was decoded in */
+    uint32_t rounds;   /* decode launches, all segments */
+    uint64_t jobs;     /* speculative decoders started, all segments */
+    double seconds;    /* wall time of the whole call */
+    double upload_s, find_s, decode_s, resolve_s, download_s; /* GPU time per stage */
+} gi_stats;
+
+/* Gets the output in stream order, always from one thread owned by the library, never two
+ * calls at once; the bytes are valid only during the call. A nonzero return stops the decode
+ * (GI_ERR_ABORTED). reference: gpuinflate/gpuinflate.h:61-63 */
+typedef int (*gi_sink)(void* user, const uint8_t* data, size_t len);
+
+/* reference: gpuinflate/gpuinflate.h:65 (returns GI_ABI_VERSION) */
+GI_API uint32_t gi_abi_version(void);
+
+/* Creates a context on cfg->device (cfg NULL: device 0, automatic sizes) and allocates its GPU
+ * and pinned host buffers. On failure *ctx is NULL and err (if given) describes the cause.
+ * reference: gpuinflate/gpuinflate.h:69, gpuinflate/gpuinflate.cu:881-907 */
+GI_API int gi_create(const gi_config* cfg, gi_ctx** ctx, char* err, size_t err_len);
+
+/* Decodes the raw Deflate stream that begins at in[0]. Bytes after the final block are
+ * allowed and are not read beyond what the stream needs; stats->in_used says where it ended.
+ * out_hint is the expected output size or 0; it only sizes the first segment. sink may be
+ * NULL (output discarded after it reaches host memory); stats may be NULL and is filled on
+ * every return. in NULL with in_size > 0 is GI_ERR_ARG; in_size 0 is GI_ERR_TRUNCATED.
+ * reference: gpuinflate/gpuinflate.h:74-75, gpuinflate/gpuinflate.cu:909-940 */
+GI_API int gi_inflate(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, uint64_t out_hint, gi_sink sink, void* user,
+                      gi_stats* stats);
+
+/* Text of the last failure on ctx, valid until the next call on ctx.
+ * reference: gpuinflate/gpuinflate.h:78 */
+GI_API const char* gi_last_error(const gi_ctx* ctx);
+
+/* Name of the context's GPU. reference: gpuinflate/gpuinflate.h:81 */
+GI_API const char* gi_device_name(const gi_ctx* ctx);
+
+/* Frees the context and its buffers. reference: gpuinflate/gpuinflate.h:83 */
+GI_API void gi_destroy(gi_ctx* ctx);
+
+/* ------------------------------------------------------------------ part 2: additions */
+
+/* CRC-32 (gzip's, reflected 0xEDB88320) and byte count mod 2^32 of the output of the last
+ * call on ctx that returned GI_OK, both computed on the GPU. No counterpart in the reference:
+ * its caller folds every sink chunk into crc32fast (src/gz.rs:207-247). */
+GI_API uint32_t gi_last_crc32(const gi_ctx* ctx);
+GI_API uint32_t gi_last_isize(const gi_ctx* ctx);
+
+/* Device-resident form: the raw Deflate stream is already in GPU memory (d_in, in_size bytes,
+ * on ctx's device) and the output goes to GPU memory (d_out, out_cap bytes). *out_size gets
+ * the output length; an output longer than out_cap returns GI_ERR_SPACE. Same error classes
+ * and in_used as gi_inflate. No counterpart in the reference (its input always comes from
+ * host memory, gpuinflate/gpuinflate.cu:672-692). */
+GI_API int gi_inflate_device(gi_ctx* ctx, const void* d_in, uint64_t in_size, void* d_out, uint64_t out_cap,
+                             uint64_t* out_size, gi_stats* stats);
+
+/* One gzip member (RFC 1952) at in[0]: header parsed as gpuzip's src/gz.rs:62-110 does, the
+ * raw stream decoded as gi_inflate does, then the trailer's CRC-32 and ISIZE checked against
+ * the values computed on the GPU (src/gz.rs:236-247 does that check on the host). A mismatch
+ * is GI_ERR_DATA. *member_size (may be NULL) gets the member's size including its trailer. */
+GI_API int gi_inflate_gzip(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, gi_sink sink, void* user,
+                           uint64_t* member_size, gi_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,62 @@
+"""CPU: the C interface library loads, exports every symbol include/gpuinflate.h declares, keeps
+interface 1's struct layouts, and rejects bad arguments before touching a GPU."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from gpuzip_gb300 import gpuinflate
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared():
+    src = open(os.path.join(ROOT, "include", "gpuinflate.h")).read()
+    return set(re.findall(r"GI_API\s+[\w\s\*]+?\b(gi_\w+)\s*\(", src))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(gpuinflate.LIB_PATH):
+        from gpuzip_gb300 import build
+
+        build.build()
+    return gpuinflate.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared()
+    assert {"gi_abi_version", "gi_create", "gi_inflate", "gi_last_error", "gi_device_name", "gi_destroy"} <= names
+    out = subprocess.run(["nm", "-D", "--defined-only", gpuinflate.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (gi_\w+)", out))
+    assert names <= exported, names - exported
+    assert exported == names, exported - names  # nothing else is exported (visibility hidden)
+    assert set(gpuinflate.EXPORTED) == names
+
+
+def test_abi_version(lib):
+    assert lib.gi_abi_version() == 1
+
+
+def test_struct_layouts_match_interface_1():
+    # gpuinflate.h of the reference: gi_config 16 bytes, gi_stats 80 (src/inflate.rs:16-39 mirrors them)
+    assert ctypes.sizeof(gpuinflate.Config) == 16
+    assert ctypes.sizeof(gpuinflate.Stats) == 80
+    assert gpuinflate.Stats.seconds.offset == 32
+
+
+def test_bad_arguments_without_gpu(lib):
+    cfg = gpuinflate.Config(8, 0, 0, 0)  # size too small
+    ctx = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(512)
+    assert lib.gi_create(ctypes.byref(cfg), ctypes.byref(ctx), err, 512) == gpuinflate.GI_ERR_ARG
+    assert ctx.value is None
+    assert b"too small" in err.value
+    assert lib.gi_create(ctypes.byref(cfg), None, err, 512) == gpuinflate.GI_ERR_ARG
+    st = gpuinflate.Stats()
+    assert lib.gi_inflate(None, b"x", 1, 0, gpuinflate.SINK(), None, ctypes.byref(st)) == gpuinflate.GI_ERR_ARG
+    assert lib.gi_last_error(None) == b"no context"
+    assert lib.gi_device_name(None) == b""
+    lib.gi_destroy(None)
