@@ -1,0 +1,337 @@
+"""Benchmark of the Deflate decode path on GB300: decompressed GB/s of one 4 GiB gzip member.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--nseg S]
+
+Workload (seeded, synthetic): one gzip member of 4096 segments of 1 MiB (4 GiB of output, the
+trailer's ISIZE wraps to 0), each segment log text / random bytes / repeated patterns with 1%
+flips / uint32 counters (p = 0.5/0.2/0.15/0.15), each at a zlib level drawn from {1, 6, 9}, all
+in ONE Deflate stream (gpuzip_gb300/workloads.py:mixed_member).
+
+One step = one full decode of the stream. `value`: the compressed stream already in GPU memory,
+the output written to GPU memory (gi_inflate_device), timed with CUDA events around each call
+(the calls are synchronous). `e2e`: the same stream through the public gzip entry point from
+pinned host memory (gi_inflate_gzip: header parse, H2D, decode, CRC-32/ISIZE checked on the GPU,
+D2H of every output byte into the library's pinned buffers); the output goes to no sink, as in
+the reference's own timing (gpuinflate/gi_test.cpp:182-190). Every step's CRC-32 and size are
+checked against the generator's.
+
+`--impl reference`: the reference's CPU decoder for this path, i.e. the oracle port of its
+sequential gi::Decoder (oracle/gi_oracle.c), on a bounded prefix of the same stream.
+Under torchrun (N > 1) every rank decodes its own copy (replicas; the path has no exchange).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "decompressed GB/s, one 4 GiB gzip member (mixed content), 1 GB300"
+CACHE = os.environ.get("GI_BENCH_CACHE", "/tmp/gpuzip_gb300_bench")
+
+
+def workload(seed, nseg):
+    """(member bytes, info) of the mixed workload, cached on local disk between runs."""
+    from gpuzip_gb300 import workloads as W
+
+    os.makedirs(CACHE, exist_ok=True)
+    path = os.path.join(CACHE, f"mixed_s{seed}_n{nseg}.gz")
+    meta = path + ".json"
+    if os.path.exists(path) and os.path.exists(meta):
+        with open(meta) as f:
+            info = json.load(f)
+        with open(path, "rb") as f:
+            return f.read(), info
+    t = time.time()
+    member, info = W.mixed_member(seed=seed, nseg=nseg)
+    info = {"crc": info["crc"], "size": info["size"], "deflate_size": info["deflate_size"],
+            "gen_seconds": time.time() - t}
+    with open(path + ".tmp", "wb") as f:
+        f.write(member)
+    os.replace(path + ".tmp", path)
+    with open(meta, "w") as f:
+        json.dump(info, f)
+    return member, info
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid=None):
+        self.rows = []
+        self.proc = None
+        self.uuid = uuid
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.uuid:
+            cmd.insert(1, f"--id={self.uuid}")
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+            self.reader.join(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel):
+    """dram bytes per launch of `kernel` from the committed ncu summary (scaled to one full
+    launch of this workload), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f)
+        return t.get(kernel, {}).get("bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_sample(body, out_bytes):
+    """The oracle port (one thread: the reference's sequential decoder) on the stream's first
+    out_bytes bytes of output: seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    lib = oracle.lib()
+    out = ctypes.create_string_buffer(out_bytes)
+    n = ctypes.c_uint64(0)
+    used = ctypes.c_uint64(0)
+    t = time.perf_counter()
+    rc = lib.oracle_inflate(body, len(body), out, out_bytes, ctypes.byref(n), ctypes.byref(used))
+    dt = time.perf_counter() - t
+    if rc not in (0, 7):
+        raise RuntimeError(f"oracle failed on the workload: {rc}")
+    return dt
+
+
+def run_reference(args, member, info, ws, rank):
+    if rank != 0:
+        return
+    body = member[10:]
+    sample = args.cpu_sample_mb << 20
+    for _ in range(args.warmup):
+        cpu_sample(body, sample)
+    times = [cpu_sample(body, sample) for _ in range(args.steps)]
+    tot = sum(times)
+    value = args.steps * sample / tot / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "GB/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot / args.steps * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": config_of(args, info),
+        "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": 1, "kind": "port",
+                         "sample": f"first {args.cpu_sample_mb} MiB of output of the same stream, decoded by the oracle "
+                                   "port of the reference's sequential gi::Decoder (one thread: a single Deflate stream "
+                                   "is sequential for it)"},
+        "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args, info):
+    return {"workload": f"one gzip member, {args.nseg} x 1 MiB segments of mixed content (seed {args.seed}), levels 1/6/9 "
+                        "in one Deflate stream",
+            "output_bytes": info["size"], "compressed_bytes": info["deflate_size"],
+            "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nseg", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--seg-out-mb", type=int, default=0)
+    ap.add_argument("--cpu-sample-mb", type=int, default=768)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="one device-resident decode, no timing (for ncu)")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    member, info = workload(args.seed, args.nseg)
+    if args.impl == "reference":
+        run_reference(args, member, info, ws, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from gpuzip_gb300 import gpuinflate
+
+    if not os.path.exists(gpuinflate.LIB_PATH):
+        import __graft_entry__
+
+        __graft_entry__.build()
+    g = gpuinflate.Gpu(local, segment_out_mb=args.seg_out_mb)
+    body = member[10:10 + info["deflate_size"]]
+    d_in = torch.frombuffer(bytearray(body), dtype=torch.uint8).cuda()
+    d_out = torch.empty(info["size"] + 4096, dtype=torch.uint8, device="cuda")
+
+    def step():
+        n, st = g.inflate_device(d_in.data_ptr(), d_in.numel(), d_out.data_ptr(), d_out.numel())
+        if n != info["size"] or g.last_crc32() != info["crc"]:
+            raise RuntimeError(f"wrong output: {n} bytes, crc {g.last_crc32():08x}, want {info['size']} {info['crc']:08x}")
+        return st, g.last_profile()
+
+    if args.profile_only:
+        step()
+        torch.cuda.synchronize()
+        return
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier = (lambda: torch.distributed.barrier()) if ws > 1 else (lambda: None)
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        pass
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    profs = []
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(uuid) as clocks:
+        for a, b in evs:
+            a.record()
+            st, pr = step()
+            b.record()
+            profs.append(pr.as_dict())
+        torch.cuda.synchronize()
+    barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_s = sum(step_ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = ws * args.steps * info["size"] / total_s / 1e9
+
+    # roofline: the kernel with the largest share of GPU time
+    kms = {k: sum(p["kernel_ms"][k] for p in profs) for k in profs[0]["kernel_ms"]}
+    top = max(kms, key=kms.get)
+    launches_of = {"decode": sum(p["decode_launches"] for p in profs), "jump": sum(p["jump_launches"] for p in profs)}
+    nl = launches_of.get(top) or sum(p["decode_launches"] for p in profs)
+    per_launch_s = kms[top] / 1e3 / nl
+    alg_bytes = sum(p["in_bytes"] + p["out_bytes"] for p in profs) / nl
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / per_launch_s / 1e9
+    roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "peak_kind": peak_kind, "traffic": traffic_per_launch(top),
+                "algorithmic_bytes_per_launch": int(alg_bytes), "launch_ms": round(per_launch_s * 1e3, 3),
+                "kernel_share": {k: round(v / sum(kms.values()), 4) for k, v in kms.items()}}
+    gpu_launches = sum(p["launches"] for p in profs)
+
+    e2e = None
+    if not args.no_e2e:
+        pinned = torch.frombuffer(bytearray(member), dtype=torch.uint8).pin_memory()
+        lib = g.lib
+        msize = ctypes.c_uint64(0)
+        stats = gpuinflate.Stats()
+
+        def e2e_step():
+            rc = lib.gi_inflate_gzip(g.ctx, ctypes.cast(pinned.data_ptr(), ctypes.c_char_p), pinned.numel(),
+                                     gpuinflate.SINK(), None, ctypes.byref(msize), ctypes.byref(stats))
+            if rc != 0 or stats.out_size != info["size"]:
+                raise RuntimeError(f"e2e failed: {rc} {lib.gi_last_error(g.ctx)}")
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        if ws > 1:
+            t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": round(ws * args.steps * info["size"] / e2e_s / 1e9, 3), "unit": "GB/s",
+               "h2d_bytes_per_step": len(member), "d2h_bytes_per_step": info["size"],
+               "path": "gi_inflate_gzip from pinned host memory, CRC-32/ISIZE checked on the GPU, output to pinned "
+                       "host buffers (no sink)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sample = args.cpu_sample_mb << 20
+        dt = cpu_sample(member[10:], sample)
+        cpu = {"value": round(sample / dt / 1e9, 4), "unit": "GB/s", "cores": 1, "kind": "port",
+               "sample": f"first {args.cpu_sample_mb} MiB of output of the same stream, oracle port of the reference's "
+                         "sequential gi::Decoder, one thread"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_s / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": config_of(args, info),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
+            "gpu_launches": gpu_launches,
+            "stages_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()},
+            "jobs_per_step": profs[0]["jobs"], "segments_per_step": st.segments,
+        }
+        print(json.dumps(line), flush=True)
+    g.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -117,18 +117,19 @@ struct Piece {
 };
 
 // launchers (each file owns its kernels)
-void launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
+// each launcher returns how many kernels it launched
+int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
                  uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, void* stream);
 int decode_blocks_per_sm();
-void launch_decode(const DecodeArgs& a, int grid, void* stream);
-void launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream);
-void launch_absolute(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t W, uint32_t* e32, int* bad,
+int launch_decode(const DecodeArgs& a, int grid, void* stream);
+int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream);
+int launch_absolute(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t W, uint32_t* e32, int* bad,
                      uint64_t bad_limit, void* stream);
-void launch_window(uint32_t* e32, const uint8_t* window, uint32_t W, void* stream);
-void launch_jump(uint32_t* e32, uint64_t n, const uint32_t* list, uint32_t* next, unsigned* nnext, uint64_t cap,
+int launch_window(uint32_t* e32, const uint8_t* window, uint32_t W, void* stream);
+int launch_jump(uint32_t* e32, uint64_t n, const uint32_t* list, uint32_t* next, unsigned* nnext, uint64_t cap,
                  void* stream);
-void launch_narrow(const uint32_t* e32, uint64_t n, uint8_t* out, void* stream);
-void launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
+int launch_narrow(const uint32_t* e32, uint64_t n, uint8_t* out, void* stream);
+int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
                 void* stream);
 uint64_t crc_scratch_words(uint64_t n);
 

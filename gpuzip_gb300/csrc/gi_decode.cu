@@ -700,8 +700,9 @@ int decode_blocks_per_sm() {
     return n > 0 ? n : 1;
 }
 
-void launch_decode(const DecodeArgs& a, int grid, void* stream) {
+int launch_decode(const DecodeArgs& a, int grid, void* stream) {
     k_decode<<<grid, NWARPS * 32, NWARPS * sizeof(Tables), (cudaStream_t)stream>>>(a);
+    return 1;
 }
 
 }  // namespace gz

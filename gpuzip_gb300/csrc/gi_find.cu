@@ -243,9 +243,9 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
 
 }  // namespace
 
-void launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
+int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
                  uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, void* stream) {
-    if (!nchunks) return;
+    if (!nchunks) return 0;
     int dev = 0, nsm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -253,6 +253,7 @@ void launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t
     uint64_t cap = (uint64_t)nsm * 8;
     k_find<<<(unsigned)(blocks < cap ? blocks : cap), FIND_WARPS * 32, 0, (cudaStream_t)stream>>>(
         (const uint32_t*)d_in, bit_lo, bit_hi, end_word, end_bit, chunk_bits, nchunks, d_first);
+    return 1;
 }
 
 }  // namespace gz

@@ -263,8 +263,9 @@ uint64_t crc_scratch_words(uint64_t n) {
     return total + 4;
 }
 
-void launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
-                void* stream) {
+int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
+               void* stream) {
+    int launches = 1;
     cudaStream_t st = (cudaStream_t)stream;
     CrcConsts k{};
     for (int s = 0; s < 5; s++) k.lane[s] = x8n_host(128ull << s);
@@ -276,11 +277,13 @@ void launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scr
         unsigned grid = (unsigned)((ntiles + 7) / 8);
         if (grid > 152 * 16) grid = 152 * 16;
         k_crc_tiles<<<grid, 256, 0, st>>>(data, ntiles, cur, k);
+        launches++;
         while (cnt > 1) {
             for (int s = 0; s < 10; s++) k.level[s] = x8n_host(item << s);
             uint64_t groups = (cnt + 1023) / 1024;
             uint32_t* nxt = cur + cnt;
             k_crc_merge<<<(unsigned)(groups < 4096 ? groups : 4096), 512, 0, st>>>(cur, cnt, nxt, k);
+            launches++;
             cur = nxt;
             cnt = groups;
             item *= 1024;
@@ -289,38 +292,46 @@ void launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scr
     (void)scratch_words;
     uint32_t tail = (uint32_t)(n - ntiles * 4096);
     k_crc_tail<<<1, 256, 0, st>>>(data, ntiles * 4096, tail, cur, x8n_host(tail), result);
+    return launches;
 }
 
-void launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream) {
-    if (n <= 0) return;
+int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream) {
+    if (n <= 0) return 0;
     k_stored<<<n < 65535 ? n : 65535, 256, 0, (cudaStream_t)stream>>>(d_in, pool, list, n);
+    return 1;
 }
 
-void launch_absolute(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t W, uint32_t* e32, int* bad,
-                     uint64_t bad_limit, void* stream) {
-    if (npieces <= 0) return;
+int launch_absolute(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t W, uint32_t* e32, int* bad,
+                    uint64_t bad_limit, void* stream) {
+    if (npieces <= 0) return 0;
+    int launches = 0;
     // blockIdx.y: the piece; blockIdx.x strides over it
     for (int p0 = 0; p0 < npieces; p0 += 65535) {
         int np = npieces - p0 < 65535 ? npieces - p0 : 65535;
         dim3 grid(8, np);
         k_absolute<<<grid, 256, 0, (cudaStream_t)stream>>>(pool, pieces + p0, W, e32, bad, bad_limit);
+        launches++;
     }
+    return launches;
 }
 
-void launch_window(uint32_t* e32, const uint8_t* window, uint32_t W, void* stream) {
-    if (!W) return;
+int launch_window(uint32_t* e32, const uint8_t* window, uint32_t W, void* stream) {
+    if (!W) return 0;
     k_window<<<blocks_for(W, 256), 256, 0, (cudaStream_t)stream>>>(e32, window, W);
+    return 1;
 }
 
-void launch_jump(uint32_t* e32, uint64_t n, const uint32_t* list, uint32_t* next, unsigned* nnext, uint64_t cap,
-                 void* stream) {
-    if (!n) return;
+int launch_jump(uint32_t* e32, uint64_t n, const uint32_t* list, uint32_t* next, unsigned* nnext, uint64_t cap,
+                void* stream) {
+    if (!n) return 0;
     k_jump<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(e32, n, list, next, nnext, cap);
+    return 1;
 }
 
-void launch_narrow(const uint32_t* e32, uint64_t n, uint8_t* out, void* stream) {
-    if (!n) return;
+int launch_narrow(const uint32_t* e32, uint64_t n, uint8_t* out, void* stream) {
+    if (!n) return 0;
     k_narrow<<<blocks_for((n + 15) / 16, 256), 256, 0, (cudaStream_t)stream>>>(e32, n, out);
+    return 1;
 }
 
 }  // namespace gz

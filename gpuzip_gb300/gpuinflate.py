@@ -28,6 +28,7 @@ EXPORTED = (
     "gi_last_isize",
     "gi_inflate_device",
     "gi_inflate_gzip",
+    "gi_last_profile",
 )
 
 
@@ -48,6 +49,21 @@ class Stats(ctypes.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Profile(ctypes.Structure):
+    """gi_profile (gpuinflate.h)"""
+
+    KINDS = ("find", "decode", "stored", "absolute", "jump", "narrow", "crc")
+    _fields_ = [("size", ctypes.c_uint32), ("launches", ctypes.c_uint32), ("kernel_ms", ctypes.c_double * 7),
+                ("decode_launches", ctypes.c_uint32), ("jump_launches", ctypes.c_uint32), ("in_bytes", ctypes.c_uint64),
+                ("out_bytes", ctypes.c_uint64), ("jobs", ctypes.c_uint64), ("extents", ctypes.c_uint64),
+                ("stored_blocks", ctypes.c_uint64)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("size", "kernel_ms")}
+        d["kernel_ms"] = dict(zip(self.KINDS, list(self.kernel_ms)))
+        return d
 
 
 SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t)
@@ -94,6 +110,8 @@ def load(path=None):
     lib.gi_inflate_device.restype = ctypes.c_int
     lib.gi_inflate_gzip.argtypes = [vp, ctypes.c_char_p, u64, SINK, vp, ctypes.POINTER(u64), ctypes.POINTER(Stats)]
     lib.gi_inflate_gzip.restype = ctypes.c_int
+    lib.gi_last_profile.argtypes = [vp, ctypes.POINTER(Profile)]
+    lib.gi_last_profile.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -193,6 +211,14 @@ class Gpu:
             if rc != GI_OK:
                 raise self._error(rc)
         return n.value, st
+
+    def last_profile(self):
+        p = Profile()
+        p.size = ctypes.sizeof(Profile)
+        rc = self.lib.gi_last_profile(self.ctx, ctypes.byref(p))
+        if rc != GI_OK:
+            raise InflateError(rc, "profile")
+        return p
 
     def last_crc32(self):
         return self.lib.gi_last_crc32(self.ctx)

@@ -115,6 +115,21 @@ GI_API int gi_inflate_device(gi_ctx* ctx, const void* d_in, uint64_t in_size, vo
 GI_API int gi_inflate_gzip(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, gi_sink sink, void* user,
                            uint64_t* member_size, gi_stats* stats);
 
+/* Where the GPU time of the last call on ctx went, per kernel kind (CUDA events around every
+ * launch on the context's stream), and what the call moved. No counterpart in the reference
+ * (its gi_stats has only the five stage times, which part 1 keeps). */
+typedef struct {
+    uint32_t size;          /* sizeof(gi_profile), set by the caller */
+    uint32_t launches;      /* kernels the call launched */
+    double kernel_ms[7];    /* find, decode, stored copies, entries, pointer jumping, narrowing, CRC-32 */
+    uint32_t decode_launches, jump_launches;
+    uint64_t in_bytes;      /* compressed bytes uploaded, all segments */
+    uint64_t out_bytes;     /* bytes produced */
+    uint64_t jobs, extents, stored_blocks;
+} gi_profile;
+
+GI_API int gi_last_profile(const gi_ctx* ctx, gi_profile* profile);
+
 #ifdef __cplusplus
 }
 #endif
