@@ -267,8 +267,7 @@ def main():
     # roofline: the kernel with the largest share of GPU time
     kms = {k: sum(p["kernel_ms"][k] for p in profs) for k in profs[0]["kernel_ms"]}
     top = max(kms, key=kms.get)
-    launches_of = {"decode": sum(p["decode_launches"] for p in profs), "jump": sum(p["jump_launches"] for p in profs)}
-    nl = launches_of.get(top) or sum(p["decode_launches"] for p in profs)
+    nl = sum(p["decode_launches"] for p in profs)  # every kernel kind runs once per segment
     per_launch_s = kms[top] / 1e3 / nl
     alg_bytes = sum(p["in_bytes"] + p["out_bytes"] for p in profs) / nl
     peak, peak_kind = peaks()
@@ -306,6 +305,8 @@ def main():
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_s = float(t.item())
         e2e = {"value": round(ws * args.steps * info["size"] / e2e_s / 1e9, 3), "unit": "GB/s",
+               "stages_s": {k: round(getattr(stats, k), 4) for k in ("upload_s", "find_s", "decode_s", "resolve_s",
+                                                                      "download_s", "seconds")},
                "h2d_bytes_per_step": len(member), "d2h_bytes_per_step": info["size"],
                "path": "gi_inflate_gzip from pinned host memory, CRC-32/ISIZE checked on the GPU, output to pinned "
                        "host buffers (no sink)"}

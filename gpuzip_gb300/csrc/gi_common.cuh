@@ -62,6 +62,8 @@ struct JobResult {
     int32_t landed;      // target index it landed on, -1: none (end of stream, stop or error)
     int32_t end_final;   // BFINAL of the block it ended in, -1 unknown
     uint32_t blocks;     // block headers read
+    uint64_t cycles;     // SM clock cycles the job took (diagnostics)
+    uint64_t hdr0;       // header of the first block it decoded symbols of (diagnostics)
 };
 
 // a run of a job's output in the pool; job k's first extent is extent k
@@ -109,6 +111,24 @@ struct DecodeArgs {
     Counters* ctr;
 };
 
+// probe points of one span: first_point + i * spacing for i < npoints, with the tables of `start`
+struct ProbeSpan {
+    Start start;
+    uint64_t first_point;
+    uint64_t spacing;
+    uint32_t npoints;
+    uint32_t out_index;  // results go to out[out_index + i]
+};
+
+struct ProbeArgs {
+    const uint8_t* in;
+    uint64_t end_word;
+    const ProbeSpan* spans;
+    int32_t nspans;
+    uint32_t lead;      // bits decoded before a point to fall into step
+    Start* out;
+};
+
 // a run of the segment's output: pool[src .. src+len) goes to output position dst
 struct Piece {
     uint64_t src;
@@ -117,18 +137,35 @@ struct Piece {
 };
 
 // launchers (each file owns its kernels)
+// a byte position whose 16-bit LEN and NLEN fields look like a stored block's (NLEN = ~LEN)
+struct StoredCand {
+    uint64_t byte;
+    uint64_t len;
+};
+
 // each launcher returns how many kernels it launched
+// d_first gets FIND_SLOTS_PER_CHUNK entries per chunk: the chunk's first block starts in bit order,
+// UINT64_MAX where there are fewer. skip (may be null): chunks flagged nonzero are not scanned
+// (they lie inside stored blocks)
+constexpr int FIND_SLOTS_PER_CHUNK = 4;
 int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
-                 uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, void* stream);
+                uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, const uint8_t* skip, void* stream);
+int launch_stored_scan(const uint8_t* d_in, uint64_t byte_lo, uint64_t byte_hi, uint64_t end_word, uint64_t end_byte,
+                       StoredCand* out, unsigned* n, unsigned cap, void* stream);
 int decode_blocks_per_sm();
 int launch_decode(const DecodeArgs& a, int grid, void* stream);
+int launch_probe(const ProbeArgs& a, int grid, void* stream);
 int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream);
-int launch_absolute(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t W, uint32_t* e32, int* bad,
-                     uint64_t bad_limit, void* stream);
-int launch_window(uint32_t* e32, const uint8_t* window, uint32_t W, void* stream);
-int launch_jump(uint32_t* e32, uint64_t n, const uint32_t* list, uint32_t* next, unsigned* nnext, uint64_t cap,
-                 void* stream);
-int launch_narrow(const uint32_t* e32, uint64_t n, uint8_t* out, void* stream);
+// the output is resolved in spans of this many positions (a multiple of 16 and at least WINDOW)
+constexpr uint64_t SPAN = 512 * 1024;
+// passes: 1 = local resolution (and the check for matches before the start), 2 = windows and bytes
+int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t total, uint32_t W,
+                   const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad, uint8_t* out, int passes,
+                   void* stream);
+int resolve_setup();  // once per device: kernel attributes (returns a cudaError_t)
+uint64_t resolve_map_slots(uint64_t seg_out_max);  // extra 16-bit slots out16 needs after the output
+int launch_next_window(const uint8_t* out, uint64_t total, const uint8_t* old, uint32_t W, uint8_t* nw, uint32_t newW,
+                       void* stream);
 int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
                 void* stream);
 uint64_t crc_scratch_words(uint64_t n);

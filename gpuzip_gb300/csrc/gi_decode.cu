@@ -372,7 +372,7 @@ __device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, in
     int lane = C.lane;
     flush_partial(o, lane);
     uint64_t want = o.cap * 2;
-    if (want < (1ull << 20)) want = 1ull << 20;
+    if (want < (64ull << 10)) want = 64ull << 10;
     if (want > (16ull << 20)) want = 16ull << 20;
     if (want < need) want = (need + 31) & ~31ull;
     unsigned long long off = 0;
@@ -405,8 +405,65 @@ __device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, in
     return true;
 }
 
+// Decodes one symbol of the current block and writes its output: 0 a literal or a match, 1 the
+// end-of-block code, -1 invalid data (no code, a length or distance symbol that does not exist,
+// or - check_refs - a match reaching before the stream's start). used: the bits it took.
+__device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int lane, bool check_refs, uint32_t& used) {
+    br.need(32);
+    uint32_t e = T.lit[(uint32_t)br.buf & ((1u << LB) - 1)];
+    if (e < (1u << 24)) {  // literal
+        int n = (int)(e & 15);
+        br.buf >>= n;
+        br.cnt -= n;
+        emit_lit(o, (e >> 8) & 255, lane);
+        used = (uint32_t)n;
+        return 0;
+    }
+    if ((e & 15) == 0) {
+        e = slow_decode(T.litc, T.lit_syms, A_LIT, br.buf, LB);
+        if (e == 0) return -1;
+        if (e < (1u << 24)) {
+            int n = (int)(e & 15);
+            br.buf >>= n;
+            br.cnt -= n;
+            emit_lit(o, (e >> 8) & 255, lane);
+            used = (uint32_t)n;
+            return 0;
+        }
+    }
+    uint32_t kind = e & (3u << 24);
+    if (kind == K_EOB) {
+        int n = (int)(e & 15);
+        br.buf >>= n;
+        br.cnt -= n;
+        used = (uint32_t)n;
+        return 1;
+    }
+    if (kind == K_BAD) return -1;
+    int n = (int)(e & 15), x = (int)((e >> 4) & 15);
+    uint32_t len = ((e >> 8) & 0xffff) + (uint32_t)((br.buf >> n) & ((1u << x) - 1));
+    br.buf >>= n + x;
+    br.cnt -= n + x;
+    br.need(32);
+    uint32_t de = T.dist[(uint32_t)br.buf & ((1u << DB) - 1)];
+    if ((de & 15) == 0) {
+        de = de == E_LONG ? slow_decode(T.distc, T.dist_syms, A_DIST, br.buf, DB) : 0;
+        if (de == 0) return -1;
+    }
+    if ((de & (3u << 24)) == K_BAD) return -1;
+    int dn = (int)(de & 15), dx = (int)((de >> 4) & 15);
+    uint32_t d = ((de >> 8) & 0xffff) + (uint32_t)((br.buf >> dn) & ((1u << dx) - 1));
+    br.buf >>= dn + dx;
+    br.cnt -= dn + dx;
+    if (check_refs && d > o.done + o.op) return -1;
+    emit_run(o, len, (uint16_t)(REF + d), lane);
+    used = (uint32_t)(n + x + dn + dx);
+    return 0;
+}
+
 __device__ void decode_job(Ctx& C, int k) {
     const int lane = C.lane;
+    const long long t_begin = clock64();
     Tables& T = *C.T;
     const Job J = C.a.jobs[k];
     const StreamDesc S = C.a.streams[J.stream];
@@ -429,6 +486,7 @@ __device__ void decode_job(Ctx& C, int k) {
     r.end_final = J.start.mode == AT_BLOCK ? -1 : J.start.final;
     r.blocks = 0;
     r.resume = J.start;
+    r.hdr0 = UINT64_MAX;
 
     Out o;
     o.base = C.a.pool + J.pool_off;
@@ -461,6 +519,7 @@ __device__ void decode_job(Ctx& C, int k) {
             r.status = S_DATA;
             r.end_bit = J.start.bit;
             r.out_len = 0;
+            r.cycles = 0;
             if (lane == 0) C.a.res[k] = r;
             return;
         }
@@ -568,17 +627,39 @@ __device__ void decode_job(Ctx& C, int k) {
         }
         // ---- the block's symbols
         const uint8_t mode = fixed ? IN_FIXED : IN_DYNAMIC;
+        if (r.hdr0 == UINT64_MAX) r.hdr0 = header;
         bool eob = false;
+        // one comparison per symbol covers the stop bit, the input's end and the next target
+        uint64_t lim2 = j.tbit < j.limit ? j.tbit : j.limit;
         for (;;) {
             uint64_t p = br.pos();
-            if (p >= j.limit) {
-                if (p > j.end_bit) {
-                    r.status = S_INPUT;
-                } else {
-                    r.status = S_STOPPED;
-                    r.resume = Start{p, header, mode, (int8_t)r.end_final, {0, 0, 0, 0, 0, 0}};
+            if (p >= lim2) {
+                if (p >= j.limit) {
+                    if (p > j.end_bit) {
+                        r.status = S_INPUT;
+                    } else {
+                        r.status = S_STOPPED;
+                        r.resume = Start{p, header, mode, (int8_t)r.end_final, {0, 0, 0, 0, 0, 0}};
+                    }
+                    break;
                 }
-                break;
+                // a target at or before this symbol boundary: land on it when it is a boundary
+                // of this block (same tables), else pass it
+                while (j.tbit < p) {
+                    j.t++;
+                    j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
+                }
+                if (j.tbit == p) {
+                    const Start& tt = j.tg[j.t];
+                    if (tt.mode == mode && tt.header == header) {
+                        r.landed = j.t;
+                        break;
+                    }
+                    j.t++;
+                    j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
+                }
+                lim2 = j.tbit < j.limit ? j.tbit : j.limit;
+                continue;
             }
             if (o.op + MAX_SYMBOL_OUT > o.cap) {
                 Start st = Start{p, header, mode, (int8_t)r.end_final, {0, 0, 0, 0, 0, 0}};
@@ -588,68 +669,27 @@ __device__ void decode_job(Ctx& C, int k) {
                     break;
                 }
             }
-            br.need(32);
-            uint32_t e = T.lit[br.buf & ((1u << LB) - 1)];
-            if (e < (1u << 24)) {  // literal
-                int n = (int)(e & 15);
-                br.buf >>= n;
-                br.cnt -= n;
-                emit_lit(o, (e >> 8) & 255, lane);
-                continue;
-            }
-            if ((e & 15) == 0) {
-                e = slow_decode(T.litc, T.lit_syms, A_LIT, br.buf, LB);
-                if (e == 0) {
-                    r.status = S_DATA;
-                    break;
-                }
-                if (e < (1u << 24)) {
-                    int n = (int)(e & 15);
-                    br.buf >>= n;
-                    br.cnt -= n;
-                    emit_lit(o, (e >> 8) & 255, lane);
-                    continue;
-                }
-            }
-            uint32_t kind = e & (3u << 24);
-            if (kind == K_EOB) {
-                int n = (int)(e & 15);
-                br.buf >>= n;
-                br.cnt -= n;
+            // a run of symbols with no per-symbol position or room checks: while at least 48 bits
+            // (the longest symbol) remain before the next check point and 258 symbols (the longest
+            // match) of room, no symbol can reach a target, the stop bit or the extent's end
+            int64_t left = (int64_t)(lim2 - p) - 48;
+            int64_t room = (int64_t)(o.cap - o.op) - (int64_t)MAX_SYMBOL_OUT;
+            int rc;
+            do {
+                uint32_t used;
+                const uint64_t op0 = o.op;
+                rc = one_symbol(T, br, o, lane, check_refs && r.blocks <= FIRST_RUN_BLOCKS, used);
+                left -= used;
+                room -= (int64_t)(o.op - op0);
+            } while (rc == 0 && left > 0 && room > 0);
+            if (rc > 0) {
                 eob = true;
                 break;
             }
-            if (kind == K_BAD) {
+            if (rc < 0) {
                 r.status = S_DATA;
                 break;
             }
-            // length
-            int n = (int)(e & 15), x = (int)((e >> 4) & 15);
-            uint32_t len = ((e >> 8) & 0xffff) + (uint32_t)((br.buf >> n) & ((1u << x) - 1));
-            br.buf >>= n + x;
-            br.cnt -= n + x;
-            br.need(32);
-            uint32_t de = T.dist[br.buf & ((1u << DB) - 1)];
-            if ((de & 15) == 0) {
-                de = de == E_LONG ? slow_decode(T.distc, T.dist_syms, A_DIST, br.buf, DB) : 0;
-                if (de == 0) {
-                    r.status = S_DATA;
-                    break;
-                }
-            }
-            if ((de & (3u << 24)) == K_BAD) {
-                r.status = S_DATA;
-                break;
-            }
-            int dn = (int)(de & 15), dx = (int)((de >> 4) & 15);
-            uint32_t d = ((de >> 8) & 0xffff) + (uint32_t)((br.buf >> dn) & ((1u << dx) - 1));
-            br.buf >>= dn + dx;
-            br.cnt -= dn + dx;
-            if (check_refs && r.blocks <= FIRST_RUN_BLOCKS && d > o.done + o.op) {
-                r.status = S_DATA;
-                break;
-            }
-            emit_run(o, len, (uint16_t)(REF + d), lane);
         }
         if (!eob) break;
         in_block = false;
@@ -666,9 +706,170 @@ __device__ void decode_job(Ctx& C, int k) {
     flush_partial(o, lane);
     r.end_bit = br.pos();
     r.out_len = o.done + o.op;
+    r.cycles = (uint64_t)(clock64() - t_begin);
     if (lane == 0) {
         C.a.ext[o.ext].len = o.op;
         C.a.res[k] = r;
+    }
+}
+
+// ---------------------------------------------------------------- probes
+//
+// Huffman codes resynchronize: decoding from an arbitrary bit soon falls onto the real symbol
+// boundaries (the reference's Decoder::probe, gpuinflate/inflate.cuh:583-648, uses the same
+// property). A probe decodes, writing nothing, from LEAD bits before a point with the tables of
+// the block the span begins in, restarting one bit later when the data makes no sense, and
+// reports the first symbol boundary at or after the point (or the block boundary there). A
+// wrong report is harmless: a decoder lands only on a position its own decode reaches with the
+// same tables. One warp takes all points of a span, so the span's tables are built once.
+
+// the tables a span starts with; header and final of its block (final -1 when unknown)
+__device__ __forceinline__ bool span_tables(Tables& T, const uint8_t* in, uint64_t end_word, const Start& s, int lane,
+                                            uint64_t& header, bool& fixed, int& final) {
+    if (s.mode == IN_FIXED) {
+        fixed_tables(T, lane);
+        header = s.header;
+        fixed = true;
+        final = s.final;
+        return true;
+    }
+    uint64_t h = s.mode == AT_BLOCK ? s.bit : s.header;
+    Bits hb;
+    hb.init(in, end_word, h);
+    final = (int)hb.get(1);
+    int type = (int)hb.get(2);
+    header = h;
+    if (type == 1) {
+        fixed_tables(T, lane);
+        fixed = true;
+        return true;
+    }
+    if (type != 2) return false;
+    fixed = false;
+    return dynamic_tables(T, hb, lane) == 0;
+}
+
+// the tables of a block whose header is known: fixed, or the dynamic header at `header`
+__device__ __forceinline__ bool block_tables(Tables& T, const uint8_t* in, uint64_t end_word, uint64_t header, bool fixed,
+                                             int lane) {
+    if (fixed) {
+        fixed_tables(T, lane);
+        return true;
+    }
+    Bits hb;
+    hb.init(in, end_word, header);
+    hb.get(1);
+    if (hb.get(2) != 2) return false;
+    return dynamic_tables(T, hb, lane) == 0;
+}
+
+__global__ void __launch_bounds__(NWARPS * 32, 4) k_probe(ProbeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tables& T = ((Tables*)smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) T.state = 0;
+    __syncwarp();
+    const uint64_t nwarps = (uint64_t)gridDim.x * NWARPS;
+    for (uint64_t w = (uint64_t)blockIdx.x * NWARPS + (threadIdx.x >> 5); w < (uint64_t)a.nspans; w += nwarps) {
+        const ProbeSpan ps = a.spans[w];
+        // base: the block a point's probe starts in (the span's, then the block the last probe
+        // ended in); cur: the block being decoded
+        uint64_t span_header = 0;
+        bool span_fixed = false;
+        int span_final = -1;
+        const bool ok = span_tables(T, a.in, a.end_word, ps.start, lane, span_header, span_fixed, span_final);
+        uint64_t base_header = span_header;
+        bool base_fixed = span_fixed;
+        int base_final = span_final;
+        bool have = ok;  // the loaded tables are base's
+        for (uint32_t i = 0; i < ps.npoints; i++) {
+            const uint64_t at = ps.first_point + (uint64_t)i * ps.spacing;
+            Start res = Start{UINT64_MAX, UINT64_MAX, AT_BLOCK, -1, {0, 0, 0, 0, 0, 0}};
+            uint64_t header = base_header;
+            bool fixed = base_fixed;
+            int final = base_final;
+            if (ok) {
+                uint64_t start = at - a.lead > ps.start.bit ? at - a.lead : ps.start.bit;
+                for (int attempt = 0; attempt < 32 && start < at && res.bit == UINT64_MAX; attempt++) {
+                    if (!have) {
+                        have = block_tables(T, a.in, a.end_word, base_header, base_fixed, lane);
+                        if (!have) break;
+                    }
+                    header = base_header;
+                    fixed = base_fixed;
+                    final = base_final;
+                    Bits br;
+                    br.init(a.in, a.end_word, start);
+                    uint64_t p;
+                    for (;;) {
+                        p = br.pos();
+                        if (p >= at) {
+                            res = Start{p, header, (uint8_t)(fixed ? IN_FIXED : IN_DYNAMIC), (int8_t)final,
+                                        {0, 0, 0, 0, 0, 0}};
+                            break;
+                        }
+                        br.need(32);
+                        uint32_t e = T.lit[br.buf & ((1u << LB) - 1)];
+                        if ((e & 15) == 0) e = slow_decode(T.litc, T.lit_syms, A_LIT, br.buf, LB);
+                        if (e == 0 || (e & (3u << 24)) == K_BAD) break;
+                        int n = (int)(e & 15);
+                        uint32_t kind = e & (3u << 24);
+                        if (kind == K_LIT) {
+                            br.buf >>= n;
+                            br.cnt -= n;
+                            continue;
+                        }
+                        if (kind == K_EOB) {
+                            br.buf >>= n;
+                            br.cnt -= n;
+                            uint64_t h = br.pos();
+                            if (h >= at) {
+                                res = Start{h, h, AT_BLOCK, -1, {0, 0, 0, 0, 0, 0}};
+                                break;
+                            }
+                            int fin = (int)br.get(1);
+                            int ty = (int)br.get(2);
+                            header = h;
+                            final = fin;
+                            have = false;  // the loaded tables are no longer base's
+                            if (ty == 1) {
+                                fixed_tables(T, lane);
+                                fixed = true;
+                            } else if (ty == 2 && dynamic_tables(T, br, lane) == 0) {
+                                fixed = false;
+                            } else {
+                                break;
+                            }
+                            continue;
+                        }
+                        int x = (int)((e >> 4) & 15);
+                        br.buf >>= n + x;
+                        br.cnt -= n + x;
+                        br.need(32);
+                        uint32_t de = T.dist[br.buf & ((1u << DB) - 1)];
+                        if ((de & 15) == 0) de = de == E_LONG ? slow_decode(T.distc, T.dist_syms, A_DIST, br.buf, DB) : 0;
+                        if (de == 0 || (de & (3u << 24)) == K_BAD) break;
+                        int dn = (int)(de & 15), dx = (int)((de >> 4) & 15);
+                        br.buf >>= dn + dx;
+                        br.cnt -= dn + dx;
+                    }
+                    start = p + 1;
+                }
+            }
+            if (res.bit != UINT64_MAX && res.mode != AT_BLOCK) {
+                // the next point starts in the block this one ended in (its tables are loaded)
+                base_header = header;
+                base_fixed = fixed;
+                base_final = final;
+                have = true;
+            } else if (base_header != span_header || base_fixed != span_fixed) {
+                base_header = span_header;
+                base_fixed = span_fixed;
+                base_final = span_final;
+                have = false;
+            }
+            if (lane == 0) a.out[ps.out_index + i] = res;
+        }
     }
 }
 
@@ -695,9 +896,16 @@ __global__ void __launch_bounds__(NWARPS * 32, 4) k_decode(DecodeArgs a) {
 
 int decode_blocks_per_sm() {
     int n = 0;
+    cudaFuncSetAttribute(k_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(NWARPS * sizeof(Tables)));
     cudaFuncSetAttribute(k_decode, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(NWARPS * sizeof(Tables)));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_decode, NWARPS * 32, NWARPS * sizeof(Tables));
     return n > 0 ? n : 1;
+}
+
+int launch_probe(const ProbeArgs& a, int grid, void* stream) {
+    if (a.nspans <= 0) return 0;
+    k_probe<<<grid, NWARPS * 32, NWARPS * sizeof(Tables), (cudaStream_t)stream>>>(a);
+    return 1;
 }
 
 int launch_decode(const DecodeArgs& a, int grid, void* stream) {

@@ -9,8 +9,11 @@
 // time; each lane computes the BTYPE/HLIT/HDIST test for the 32 bit offsets of its word at once
 // as bit-sliced masks (a dozen shifts and ANDs instead of 32 tests), runs the code-length-code
 // test on the survivors, and the warp compacts the survivors in bit order through a ballot
-// prefix. Full checks then run 32 candidates at a time, one per lane, and the lowest passing
-// lane (a ballot) is the chunk's first start; the warp stops scanning the chunk there.
+// prefix. Full checks then run 32 candidates at a time, one per lane; passing lanes (a ballot)
+// are kept in bit order, up to four per chunk (the reference keeps one, and misses the second
+// of two blocks that start in one chunk, which then gets no decoder of its own).
+// Chunks of 4 KiB hold about 30 such candidates in real data (the reference measured 1 in
+// 1,100 bit positions surviving the cheap tests), so the list usually drains once per chunk.
 #include <cuda_runtime.h>
 
 #include "gi_common.cuh"
@@ -170,21 +173,54 @@ __device__ __forceinline__ bool cl_code_complete(uint64_t v1, uint64_t v2) {
     return sum == 128;
 }
 
+// Candidates that pass the cheap tests queue up in bit order in the warp's shared-memory list and
+// are verified 32 at a time (one per lane), so the expensive check runs on full warps; the list
+// is drained whenever it holds a full batch, and the first batch with a pass gives the chunk's
+// first start (every earlier candidate was verified before it).
+constexpr int LIST = 1024 + 64;
+constexpr int FIND_SLOTS = 4;  // block starts kept per chunk (a short block can share a chunk with the next)
+
 __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __restrict__ w, uint64_t bit_lo,
                                                           uint64_t bit_hi, uint64_t end_word, uint64_t end_bit,
                                                           uint32_t chunk_bits, uint64_t nchunks,
-                                                          uint64_t* __restrict__ first) {
-    __shared__ uint16_t cand[FIND_WARPS][1024];
+                                                          uint64_t* __restrict__ first,
+                                                          const uint8_t* __restrict__ skip) {
+    __shared__ uint32_t cand[FIND_WARPS][LIST];  // candidate bit, relative to the chunk's first word
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t* list = cand[wib];
     const uint64_t nwarps = (uint64_t)gridDim.x * FIND_WARPS;
     for (uint64_t c = (uint64_t)blockIdx.x * FIND_WARPS + wib; c < nchunks; c += nwarps) {
         uint64_t cb = bit_lo + c * chunk_bits;
         uint64_t lo = cb > bit_lo ? cb : bit_lo + 1;  // candidates are strictly after bit_lo
         uint64_t hi = cb + chunk_bits < bit_hi ? cb + chunk_bits : bit_hi;
-        uint64_t found = UINT64_MAX;
-        if (lo < hi) {
-            uint64_t w0 = lo >> 5, w1 = (hi + 31) >> 5;
-            for (uint64_t ws = w0; ws < w1 && found == UINT64_MAX; ws += 32) {
+        int nfound = 0;
+        uint64_t found = UINT64_MAX;  // lane j < FIND_SLOTS holds hit j
+        if (lo < hi && !(skip && skip[c])) {
+            const uint64_t w0 = lo >> 5, w1 = (hi + 31) >> 5;
+            int nlist = 0;
+            // verifies list[0 .. n) in batches of 32 (n a multiple of 32 unless final), keeping the
+            // hits in bit order; true once FIND_SLOTS hits are kept
+            auto drain = [&](int n) -> bool {
+                for (int b0 = 0; b0 < n; b0 += 32) {
+                    bool ok = false;
+                    uint64_t bit = 0;
+                    if (b0 + lane < n) {
+                        bit = w0 * 32 + list[b0 + lane];
+                        ok = verify_header(w, end_word, end_bit, bit);
+                    }
+                    uint32_t bal = __ballot_sync(FULL, ok);
+                    while (bal && nfound < FIND_SLOTS) {
+                        uint64_t b = __shfl_sync(FULL, bit, __ffs(bal) - 1);
+                        if (lane == nfound) found = b;
+                        nfound++;
+                        bal &= bal - 1;
+                    }
+                    if (nfound == FIND_SLOTS) return true;
+                }
+                return false;
+            };
+            bool done = false;
+            for (uint64_t ws = w0; ws < w1 && !done; ws += 32) {
                 uint64_t wi = ws + lane;
                 uint32_t mask = 0;
                 if (wi < w1) {
@@ -199,6 +235,7 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
                     uint64_t base = wi * 32;
                     if (base < lo) mask &= ~0u << (uint32_t)(lo - base);
                     if (base + 32 > hi) mask &= (1u << (uint32_t)(hi - base)) - 1;
+
                     uint32_t keep = 0, mm = mask;
                     while (mm) {
                         int o = __ffs(mm) - 1;
@@ -209,7 +246,7 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
                     }
                     mask = keep;
                 }
-                // survivors, in bit order, into the warp's list
+                // survivors, in bit order, appended to the warp's list
                 int n = __popc(mask), incl = n;
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
@@ -217,34 +254,67 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
                     if (lane >= d) incl += v;
                 }
                 int total = __shfl_sync(FULL, incl, 31);
-                int j = incl - n;
-                for (uint32_t mm = mask; mm; mm &= mm - 1) cand[wib][j++] = (uint16_t)((lane << 5) | (__ffs(mm) - 1));
+                int j = nlist + incl - n;
+                uint32_t rel = (uint32_t)((wi - w0) * 32);
+                for (uint32_t mm = mask; mm; mm &= mm - 1) list[j++] = rel + (uint32_t)(__ffs(mm) - 1);
+                nlist += total;
                 __syncwarp();
-                for (int b0 = 0; b0 < total; b0 += 32) {
-                    bool ok = false;
-                    uint64_t bit = 0;
-                    if (b0 + lane < total) {
-                        uint32_t e = cand[wib][b0 + lane];
-                        bit = (ws + (e >> 5)) * 32 + (e & 31);
-                        ok = verify_header(w, end_word, end_bit, bit);
-                    }
-                    uint32_t bal = __ballot_sync(FULL, ok);
-                    if (bal) {
-                        found = __shfl_sync(FULL, bit, __ffs(bal) - 1);
-                        break;
+                if (nlist >= 32) {
+                    int full = nlist & ~31;
+                    done = drain(full);
+                    if (!done) {
+                        // keep the unverified tail at the front
+                        int rest = nlist - full;
+                        uint32_t v = lane < rest ? list[full + lane] : 0;
+                        __syncwarp();
+                        if (lane < rest) list[lane] = v;
+                        nlist = rest;
+                        __syncwarp();
                     }
                 }
-                __syncwarp();
+            }
+            if (!done && nlist) drain(nlist);
+        }
+        if (lane < FIND_SLOTS) first[c * FIND_SLOTS + lane] = found;
+    }
+}
+
+// Stored-block signatures: every byte position in [byte_lo, byte_hi) whose 16-bit LEN is
+// followed by NLEN = ~LEN (RFC 1951 3.2.4). One thread per 32-bit word, four positions each;
+// hits are rare (one per stored block, and 1 in 65,536 positions of other data).
+__global__ void k_stored_scan(const uint32_t* __restrict__ w, uint64_t byte_lo, uint64_t byte_hi, uint64_t end_word,
+                              uint64_t end_byte, StoredCand* __restrict__ out, unsigned* __restrict__ n, unsigned cap) {
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t wi = (byte_lo >> 2) + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; wi * 4 < byte_hi; wi += stride) {
+        uint64_t v = (uint64_t)ldw(w, wi, end_word) | (uint64_t)ldw(w, wi + 1, end_word) << 32;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t len = (uint32_t)(v >> (8 * k)) & 0xffff;
+            uint32_t nlen = (uint32_t)(v >> (8 * k + 16)) & 0xffff;
+            uint64_t byte = wi * 4 + k;
+            if (len == (~nlen & 0xffff) && byte >= byte_lo && byte < byte_hi && byte + 4 + len <= end_byte) {
+                unsigned q = atomicAdd(n, 1u);
+                if (q < cap) out[q] = StoredCand{byte, len};
             }
         }
-        if (lane == 0) first[c] = found;
     }
 }
 
 }  // namespace
 
+int launch_stored_scan(const uint8_t* d_in, uint64_t byte_lo, uint64_t byte_hi, uint64_t end_word, uint64_t end_byte,
+                       StoredCand* out, unsigned* n, unsigned cap, void* stream) {
+    if (byte_hi <= byte_lo) return 0;
+    uint64_t words = (byte_hi - byte_lo) / 4 + 2;
+    uint64_t blocks = (words + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_stored_scan<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>((const uint32_t*)d_in, byte_lo, byte_hi, end_word,
+                                                                       end_byte, out, n, cap);
+    return 1;
+}
+
 int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
-                 uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, void* stream) {
+                uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, const uint8_t* skip, void* stream) {
     if (!nchunks) return 0;
     int dev = 0, nsm = 1;
     cudaGetDevice(&dev);
@@ -252,7 +322,7 @@ int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t 
     uint64_t blocks = (nchunks + FIND_WARPS - 1) / FIND_WARPS;
     uint64_t cap = (uint64_t)nsm * 8;
     k_find<<<(unsigned)(blocks < cap ? blocks : cap), FIND_WARPS * 32, 0, (cudaStream_t)stream>>>(
-        (const uint32_t*)d_in, bit_lo, bit_hi, end_word, end_bit, chunk_bits, nchunks, d_first);
+        (const uint32_t*)d_in, bit_lo, bit_hi, end_word, end_bit, chunk_bits, nchunks, d_first, skip);
     return 1;
 }
 

@@ -1,13 +1,22 @@
 // gi_resolve.cu - from decoded symbols to bytes, and the CRC-32 of the bytes.
 //
-// The resolution scheme is the reference's (gpuinflate/gpuinflate.cu:366-421): every output
-// position becomes a 32-bit entry, either LIT | byte or the absolute position it copies (the
-// 32 KiB window before the segment sits in front), a reference before the stream's start is
-// invalid data, and pointer jumping (up to 8 hops per entry per round, in place, the unresolved
-// entries carried to the next round in a list) resolves every chain.
-// Stored blocks skipped by the decoders are copied here 16 bytes of output at a time.
-// CRC-32 is computed from the output bytes: each warp takes 4 KiB (128 bytes per lane,
-// bytewise table in shared memory), lane CRCs are merged by the GF(2) identity
+// The decoders leave one 16-bit symbol per output position: a byte, or REF + d for "the byte d
+// back" (gpuinflate/inflate.cuh:31). The reference resolves those by writing a 32-bit entry per
+// position and pointer jumping over all of them (gpuinflate/gpuinflate.cu:366-421); on text,
+// where most bytes are copies of copies hundreds deep, that costs several rounds of dependent
+// gathers per byte. Here the output is cut into spans (512 KiB) and resolved in three passes
+// that never follow a chain through memory:
+//   1. k_local, one block per span, walks the span in order in tiles of 2048 positions: a copy
+//      whose source is in an earlier tile reads that tile's (already resolved) value, a copy
+//      inside the tile is resolved by pointer doubling in shared memory, and a copy that
+//      reaches before the span becomes a marker 256 + m: "byte m of the span's entry window"
+//      (the 32 KiB before the span). A copy before the stream's start sets `bad`.
+//   2. k_windows, one block, walks the spans in order: span s's entry window is span s-1's last
+//      32 KiB with its markers looked up in span s-1's entry window (one 32 KiB gather a span).
+//   3. k_final, parallel over every position: a byte, or its span's window byte.
+// Stored blocks skipped by the decoders are copied into the symbol pool first, 8 symbols (16
+// bytes) per store. CRC-32 is computed from the output bytes: each warp takes 4 KiB (128 bytes
+// per lane, bytewise table in shared memory), lane CRCs are merged by the GF(2) identity
 //     crc(A || B) = crc(A) * x^(8|B|) mod P  xor  crc(B)
 // (carry-less multiplication modulo the CRC polynomial), then 4 KiB CRCs are merged 1024 at a
 // time by the same identity until one is left. The multipliers x^(8n) for the fixed sizes are
@@ -19,7 +28,6 @@
 namespace gz {
 namespace {
 
-constexpr int HOPS = 8;
 constexpr uint32_t POLY = 0xEDB88320u;
 
 unsigned blocks_for(uint64_t n, unsigned per) {
@@ -53,73 +61,294 @@ __global__ void k_stored(const uint8_t* __restrict__ in, uint16_t* __restrict__ 
     }
 }
 
-// ---------------------------------------------------------------- entries
+// ---------------------------------------------------------------- resolution
 
-__global__ void k_window(uint32_t* e32, const uint8_t* window, uint32_t n) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) e32[i] = LIT | window[i];
+constexpr int R1_THREADS = 512;
+constexpr int TILE = 2048;  // positions per tile: 4 per thread
+constexpr int TPT = TILE / R1_THREADS;
+constexpr uint16_t PENDING = 0xFFFF;
+
+// pass 1: every span resolved on its own (see the file comment). Thread t owns positions
+// 4t..4t+3 of a tile, so its four symbols come from one piece (almost always) and leave in one
+// 8-byte store; the pieces a tile touches are staged in shared memory.
+constexpr int TILE_PIECES = 64;
+
+__device__ __forceinline__ int piece_of(const Piece* tp, int ntp, const Piece* __restrict__ pieces, int npieces,
+                                        uint64_t p) {
+    // in the staged list (ntp > 0), else the global list by binary search; returns the index into the
+    // list searched (staged index when ntp > 0)
+    if (ntp > 0) {
+        int j = 0;
+        while (j + 1 < ntp && p >= tp[j + 1].dst) j++;
+        return j;
+    }
+    int lo = 0, hi = npieces - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pieces[mid].dst <= p) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
-// every position of every piece as LIT | byte or the absolute position it copies. bad_limit:
-// only references at output positions below it count as "before the start" (positions are
-// counted from the window's start)
-__global__ void k_absolute(const uint16_t* __restrict__ pool, const Piece* __restrict__ pieces, uint64_t W,
-                           uint32_t* __restrict__ e32, int* bad, uint64_t bad_limit) {
-    Piece p = pieces[blockIdx.y];
-    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.len; i += stride) {
-        uint32_t v = pool[p.src + i];
-        uint64_t pos = W + p.dst + i;
-        uint32_t e = LIT | v;
-        if (v > REF) {
-            uint64_t d = v - REF;
-            if (d <= pos) {
-                e = (uint32_t)(pos - d);
+__global__ void __launch_bounds__(R1_THREADS) k_local(const uint16_t* __restrict__ pool, const Piece* __restrict__ pieces,
+                                                      int npieces, uint64_t total, uint64_t span, uint32_t W,
+                                                      uint16_t* out16, int* bad) {
+    __shared__ volatile uint16_t val[TILE];
+    __shared__ volatile uint16_t ptr[TILE];
+    __shared__ Piece tp[TILE_PIECES];
+    __shared__ int ntp, pcur;
+    const uint64_t nspans = (total + span - 1) / span;
+    for (uint64_t sp = blockIdx.x; sp < nspans; sp += gridDim.x) {
+        const uint64_t s0 = sp * span, s1 = s0 + span < total ? s0 + span : total;
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = npieces - 1;  // the last piece with dst <= s0
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (pieces[mid].dst <= s0) lo = mid;
+                else hi = mid - 1;
+            }
+            pcur = lo;
+        }
+        for (uint64_t tb = s0; tb < s1; tb += TILE) {
+            const int n = (int)(s1 - tb < (uint64_t)TILE ? s1 - tb : (uint64_t)TILE);
+            __syncthreads();
+            if (threadIdx.x == 0) {  // the pieces overlapping [tb, tb + n)
+                int pc = pcur;
+                while (tb >= pieces[pc].dst + pieces[pc].len) pc++;
+                pcur = pc;
+                int m = 0;
+                while (m < TILE_PIECES && pc + m < npieces && pieces[pc + m].dst < tb + n) {
+                    tp[m] = pieces[pc + m];
+                    m++;
+                }
+                ntp = (pc + m < npieces && pieces[pc + m].dst < tb + n) ? 0 : m;  // 0: too many, search globally
+            }
+            __syncthreads();
+            const int m = ntp;
+            const int i0 = threadIdx.x * TPT;
+            uint32_t v[TPT];
+            int j = -1;
+            Piece pc{};
+#pragma unroll
+            for (int k = 0; k < TPT; k++) {
+                v[k] = 0;
+                if (i0 + k < n) {
+                    uint64_t p = tb + i0 + k;
+                    if (j < 0 || p >= pc.dst + pc.len) {
+                        j = piece_of(tp, m, pieces, npieces, p);
+                        pc = m > 0 ? tp[j] : pieces[j];
+                    }
+                    v[k] = pool[pc.src + (p - pc.dst)];
+                }
+            }
+            uint16_t r[TPT], q[TPT];
+            int64_t g[TPT];
+#pragma unroll
+            for (int k = 0; k < TPT; k++) {
+                const int i = i0 + k;
+                uint64_t p = tb + i;
+                r[k] = (uint16_t)v[k];
+                q[k] = (uint16_t)i;
+                g[k] = -1;
+                if (i < n && v[k] > REF) {
+                    int64_t src = (int64_t)p - (int64_t)(v[k] - REF);
+                    if (src < (int64_t)s0) {
+                        if (src < -(int64_t)W) {
+                            *bad = 1;  // a match before the stream's start
+                            r[k] = 0;
+                        } else {
+                            r[k] = (uint16_t)(256 + (src - ((int64_t)s0 - (int64_t)WINDOW)));
+                        }
+                    } else if ((uint64_t)src < tb) {
+                        g[k] = src;
+                    } else {
+                        r[k] = PENDING;
+                        q[k] = (uint16_t)((uint64_t)src - tb);
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < TPT; k++)
+                if (g[k] >= 0) r[k] = out16[g[k]];
+#pragma unroll
+            for (int k = 0; k < TPT; k++) {
+                if (i0 + k < n) {
+                    val[i0 + k] = r[k];
+                    ptr[i0 + k] = q[k];
+                }
+            }
+            __syncthreads();
+            // copies inside the tile: pointer doubling until every chain reached a value
+            for (int round = 0; round < TILE; round++) {
+                int pend = 0;
+#pragma unroll
+                for (int k = 0; k < TPT; k++) {
+                    int i = i0 + k;
+                    if (i < n && val[i] == PENDING) {
+                        uint16_t qq = ptr[i];
+                        uint16_t vq = val[qq];
+                        if (vq != PENDING) {
+                            val[i] = vq;
+                        } else {
+                            ptr[i] = ptr[qq];
+                            pend = 1;
+                        }
+                    }
+                }
+                if (!__syncthreads_or(pend)) break;
+            }
+            if (i0 + TPT <= n) {
+                uint2 w2;
+                w2.x = (uint32_t)val[i0] | (uint32_t)val[i0 + 1] << 16;
+                w2.y = (uint32_t)val[i0 + 2] | (uint32_t)val[i0 + 3] << 16;
+                *(uint2*)(out16 + tb + i0) = w2;
             } else {
-                e = LIT;
-                if (pos < bad_limit) *bad = 1;
+                for (int k = 0; k < TPT; k++)
+                    if (i0 + k < n) out16[tb + i0 + k] = val[i0 + k];
             }
         }
-        e32[pos] = e;
+        __syncthreads();
     }
 }
 
-__device__ __forceinline__ uint32_t jump(const uint32_t* e32, uint32_t e) {
-#pragma unroll 1
-    for (int h = 0; h < HOPS && !(e & LIT); h++) e = e32[e];
-    return e;
-}
+// pass 2: the entry window of every span. window[s+1] = M_s(window[s]), where M_s is span s's
+// last 32 KiB of pass-1 values (a byte, or 256 + an index into window[s]). The chain over spans
+// is a scan over these gather maps, done in three phases over groups of L spans:
+//   compose: per group, C_g = M_{gL+L-1} o ... o M_{gL} (maps compose into a map of the same form);
+//   chain:   one block walks the groups: window[(g+1)L] = C_g(window[gL]);
+//   fill:    per group, window[gL+1 .. gL+L-1] one after the other from window[gL].
+// Serial steps: 2L + G instead of the span count. Each thread owns 32 consecutive positions.
+constexpr int WT = 1024;               // threads of the window kernels
+constexpr int WPER = WINDOW / WT;      // 32 positions per thread
 
-__global__ void k_jump(uint32_t* e32, uint64_t n, const uint32_t* list, uint32_t* next, unsigned* nnext, uint64_t cap) {
-    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    uint32_t i = list ? list[t] : (uint32_t)t;
-    uint32_t e = e32[i];
-    if (e & LIT) return;
-    e = jump(e32, e);
-    e32[i] = e;
-    if (!(e & LIT)) {
-        unsigned q = atomicAdd(nnext, 1u);
-        if (q < cap) next[q] = i;
+__device__ __forceinline__ void load_map(const uint16_t* src, uint16_t (&v)[WPER]) {
+    const uint4* p = (const uint4*)(src + threadIdx.x * WPER);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        uint4 x = p[q];
+        uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            v[q * 8 + 2 * k] = (uint16_t)(w[k] & 0xffff);
+            v[q * 8 + 2 * k + 1] = (uint16_t)(w[k] >> 16);
+        }
     }
 }
 
-// bytes of entries, 16 per thread
-__global__ void k_narrow(const uint32_t* __restrict__ e32, uint64_t n, uint8_t* __restrict__ out) {
-    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint64_t i = t * 16;
-    if (i + 16 <= n && ((uintptr_t)(out + i) & 15) == 0 && ((uintptr_t)(e32 + i) & 15) == 0) {
-        const uint4* s = (const uint4*)(e32 + i);
-        uint4 a = s[0], b = s[1], c = s[2], d = s[3];
-        uint4 q;
-        q.x = (a.x & 255) | (a.y & 255) << 8 | (a.z & 255) << 16 | (a.w & 255) << 24;
-        q.y = (b.x & 255) | (b.y & 255) << 8 | (b.z & 255) << 16 | (b.w & 255) << 24;
-        q.z = (c.x & 255) | (c.y & 255) << 8 | (c.z & 255) << 16 | (c.w & 255) << 24;
-        q.w = (d.x & 255) | (d.y & 255) << 8 | (d.z & 255) << 16 | (d.w & 255) << 24;
-        *(uint4*)(out + i) = q;
+// C_g for every group (one block per group); maps[g] gets the composed map
+__global__ void __launch_bounds__(WT) k_compose(const uint16_t* __restrict__ out16, uint64_t nmaps, uint64_t span,
+                                                uint64_t L, uint16_t* __restrict__ maps) {
+    extern __shared__ __align__(16) uint16_t R[];  // the running composition
+    const uint64_t g = blockIdx.x, m0 = g * L, m1 = m0 + L < nmaps ? m0 + L : nmaps;
+    uint16_t v[WPER];
+    load_map(out16 + (m0 + 1) * span - WINDOW, v);
+#pragma unroll
+    for (int k = 0; k < WPER; k++) R[threadIdx.x * WPER + k] = v[k];
+    __syncthreads();
+    for (uint64_t m = m0 + 1; m < m1; m++) {
+        load_map(out16 + (m + 1) * span - WINDOW, v);
+#pragma unroll
+        for (int k = 0; k < WPER; k++) v[k] = v[k] < 256 ? v[k] : R[v[k] - 256];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < WPER; k++) R[threadIdx.x * WPER + k] = v[k];
+        __syncthreads();
+    }
+    uint4* dst = (uint4*)(maps + g * WINDOW + threadIdx.x * WPER);
+    const uint4* srcv = (const uint4*)(R + threadIdx.x * WPER);
+#pragma unroll
+    for (int q = 0; q < 4; q++) dst[q] = srcv[q];
+}
+
+// applies a map to a window in shared memory (in place across a barrier), and stores the result
+__device__ __forceinline__ void apply_map(const uint16_t (&v)[WPER], uint8_t* win, uint8_t* out_global) {
+    uint8_t b[WPER];
+#pragma unroll
+    for (int k = 0; k < WPER; k++) b[k] = v[k] < 256 ? (uint8_t)v[k] : win[v[k] - 256];
+    __syncthreads();
+    uint32_t pk[WPER / 4];
+#pragma unroll
+    for (int k = 0; k < WPER / 4; k++)
+        pk[k] = (uint32_t)b[4 * k] | (uint32_t)b[4 * k + 1] << 8 | (uint32_t)b[4 * k + 2] << 16 | (uint32_t)b[4 * k + 3] << 24;
+    uint4* ws = (uint4*)(win + threadIdx.x * WPER);
+    uint4* wg = (uint4*)(out_global + threadIdx.x * WPER);
+    ws[0] = wg[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    ws[1] = wg[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    __syncthreads();
+}
+
+// window[0] from the segment's window, then window[gL] for every group (one block)
+__global__ void __launch_bounds__(WT) k_chain(const uint16_t* __restrict__ maps, uint64_t ngroups, uint64_t L,
+                                              uint64_t nspans, const uint8_t* __restrict__ seg_window, uint32_t W,
+                                              uint8_t* __restrict__ windows) {
+    __shared__ __align__(16) uint8_t win[WINDOW];
+    for (int j = threadIdx.x; j < (int)WINDOW; j += WT) {
+        uint8_t b = j >= (int)(WINDOW - W) ? seg_window[j - (WINDOW - W)] : 0;
+        win[j] = b;
+        windows[j] = b;
+    }
+    __syncthreads();
+    for (uint64_t g = 0; g + 1 < ngroups && (g + 1) * L < nspans; g++) {
+        uint16_t v[WPER];
+        load_map(maps + g * WINDOW, v);
+        apply_map(v, win, windows + (g + 1) * L * WINDOW);
+    }
+}
+
+// window[gL+1 .. gL+L-1] (one block per group)
+__global__ void __launch_bounds__(WT) k_fill(const uint16_t* __restrict__ out16, uint64_t nspans, uint64_t span,
+                                             uint64_t L, uint8_t* __restrict__ windows) {
+    __shared__ __align__(16) uint8_t win[WINDOW];
+    const uint64_t s0 = blockIdx.x * L;
+    const uint4* src = (const uint4*)(windows + s0 * WINDOW + threadIdx.x * WPER);
+    uint4* ws = (uint4*)(win + threadIdx.x * WPER);
+    ws[0] = src[0];
+    ws[1] = src[1];
+    __syncthreads();
+    for (uint64_t s = s0 + 1; s < s0 + L && s < nspans; s++) {
+        uint16_t v[WPER];
+        load_map(out16 + s * span - WINDOW, v);
+        apply_map(v, win, windows + s * WINDOW);
+    }
+}
+
+// pass 3: bytes, 16 per thread
+__global__ void k_final(const uint16_t* __restrict__ out16, uint64_t total, uint64_t span,
+                        const uint8_t* __restrict__ windows, uint8_t* __restrict__ out) {
+    uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * 16;
+    if (i >= total) return;
+    if (i + 16 <= total) {
+        const uint4* s = (const uint4*)(out16 + i);
+        uint4 a = s[0], b = s[1];
+        uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        const uint8_t* win = windows + (i / span) * WINDOW;  // 16 positions never straddle a span
+        uint32_t q[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t lo = w[2 * k] & 0xffff, hi = w[2 * k] >> 16, lo2 = w[2 * k + 1] & 0xffff, hi2 = w[2 * k + 1] >> 16;
+            uint32_t b0 = lo < 256 ? lo : win[lo - 256];
+            uint32_t b1 = hi < 256 ? hi : win[hi - 256];
+            uint32_t b2 = lo2 < 256 ? lo2 : win[lo2 - 256];
+            uint32_t b3 = hi2 < 256 ? hi2 : win[hi2 - 256];
+            q[k] = b0 | b1 << 8 | b2 << 16 | b3 << 24;
+        }
+        *(uint4*)(out + i) = make_uint4(q[0], q[1], q[2], q[3]);
     } else {
-        for (uint64_t k = i; k < n && k < i + 16; k++) out[k] = (uint8_t)e32[k];
+        for (uint64_t k = i; k < total; k++) {
+            uint32_t v = out16[k];
+            out[k] = v < 256 ? (uint8_t)v : windows[(k / span) * WINDOW + v - 256];
+        }
     }
+}
+
+// the window for the next segment: the last 32 KiB of (old window ++ this segment's output)
+__global__ void k_next_window(const uint8_t* __restrict__ out, uint64_t total, const uint8_t* __restrict__ old,
+                              uint32_t W, uint8_t* __restrict__ nw, uint32_t newW) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= newW) return;
+    int64_t pos = (int64_t)total - (int64_t)newW + j;  // in this segment's output; negative: in the old window
+    nw[j] = pos >= 0 ? out[pos] : old[(int64_t)W + pos];
 }
 
 // ---------------------------------------------------------------- CRC-32
@@ -301,36 +530,56 @@ int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, i
     return 1;
 }
 
-int launch_absolute(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t W, uint32_t* e32, int* bad,
-                    uint64_t bad_limit, void* stream) {
-    if (npieces <= 0) return 0;
+int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t total, uint32_t W,
+                   const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad, uint8_t* out, int passes,
+                   void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!total || npieces <= 0) return 0;
+    uint64_t nspans = (total + SPAN - 1) / SPAN;
     int launches = 0;
-    // blockIdx.y: the piece; blockIdx.x strides over it
-    for (int p0 = 0; p0 < npieces; p0 += 65535) {
-        int np = npieces - p0 < 65535 ? npieces - p0 : 65535;
-        dim3 grid(8, np);
-        k_absolute<<<grid, 256, 0, (cudaStream_t)stream>>>(pool, pieces + p0, W, e32, bad, bad_limit);
+    if (passes & 1) {
+        int dev = 0, nsm = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        uint64_t grid = nspans < (uint64_t)nsm * 4 ? nspans : (uint64_t)nsm * 4;
+        k_local<<<(unsigned)grid, R1_THREADS, 0, st>>>(pool, pieces, npieces, total, SPAN, W, out16, bad);
         launches++;
+    }
+    if (passes & 2) {
+        // groups of L spans: L about sqrt(spans) balances the three phases
+        uint64_t L = 1;
+        while (L * L < nspans) L++;
+        uint64_t ngroups = (nspans + L - 1) / L;
+        uint64_t nmaps = nspans - 1;  // M_s for s < nspans - 1
+        uint16_t* maps = out16 + ((total + 63) & ~63ull);
+        if (nmaps) {
+            k_compose<<<(unsigned)((nmaps + L - 1) / L), WT, 2 * WINDOW, st>>>(out16, nmaps, SPAN, L, maps);
+            launches++;
+        }
+        k_chain<<<1, WT, 0, st>>>(maps, ngroups, L, nspans, seg_window, W, windows);
+        k_fill<<<(unsigned)ngroups, WT, 0, st>>>(out16, nspans, SPAN, L, windows);
+        k_final<<<blocks_for((total + 15) / 16, 256), 256, 0, st>>>(out16, total, SPAN, windows, out);
+        launches += 3;
     }
     return launches;
 }
 
-int launch_window(uint32_t* e32, const uint8_t* window, uint32_t W, void* stream) {
-    if (!W) return 0;
-    k_window<<<blocks_for(W, 256), 256, 0, (cudaStream_t)stream>>>(e32, window, W);
-    return 1;
+int resolve_setup() {
+    return (int)cudaFuncSetAttribute(k_compose, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * WINDOW);
 }
 
-int launch_jump(uint32_t* e32, uint64_t n, const uint32_t* list, uint32_t* next, unsigned* nnext, uint64_t cap,
-                void* stream) {
-    if (!n) return 0;
-    k_jump<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(e32, n, list, next, nnext, cap);
-    return 1;
+// 16-bit slots after the segment's symbols that hold the composed maps (one per group)
+uint64_t resolve_map_slots(uint64_t seg_out_max) {
+    uint64_t nspans = (seg_out_max + SPAN - 1) / SPAN + 1;
+    uint64_t L = 1;
+    while (L * L < nspans) L++;
+    return 64 + ((nspans + L - 1) / L + 1) * WINDOW;
 }
 
-int launch_narrow(const uint32_t* e32, uint64_t n, uint8_t* out, void* stream) {
-    if (!n) return 0;
-    k_narrow<<<blocks_for((n + 15) / 16, 256), 256, 0, (cudaStream_t)stream>>>(e32, n, out);
+int launch_next_window(const uint8_t* out, uint64_t total, const uint8_t* old, uint32_t W, uint8_t* nw, uint32_t newW,
+                       void* stream) {
+    if (!newW) return 0;
+    k_next_window<<<blocks_for(newW, 256), 256, 0, (cudaStream_t)stream>>>(out, total, old, W, nw, newW);
     return 1;
 }
 

@@ -54,11 +54,11 @@ class Stats(ctypes.Structure):
 class Profile(ctypes.Structure):
     """gi_profile (gpuinflate.h)"""
 
-    KINDS = ("find", "decode", "stored", "absolute", "jump", "narrow", "crc")
+    KINDS = ("find", "decode", "stored", "local", "windows", "next_window", "crc")
     _fields_ = [("size", ctypes.c_uint32), ("launches", ctypes.c_uint32), ("kernel_ms", ctypes.c_double * 7),
-                ("decode_launches", ctypes.c_uint32), ("jump_launches", ctypes.c_uint32), ("in_bytes", ctypes.c_uint64),
+                ("decode_launches", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("in_bytes", ctypes.c_uint64),
                 ("out_bytes", ctypes.c_uint64), ("jobs", ctypes.c_uint64), ("extents", ctypes.c_uint64),
-                ("stored_blocks", ctypes.c_uint64)]
+                ("stored_blocks", ctypes.c_uint64), ("probes", ctypes.c_uint64)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("size", "kernel_ms")}

@@ -121,11 +121,13 @@ GI_API int gi_inflate_gzip(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, gi_
 typedef struct {
     uint32_t size;          /* sizeof(gi_profile), set by the caller */
     uint32_t launches;      /* kernels the call launched */
-    double kernel_ms[7];    /* find, decode, stored copies, entries, pointer jumping, narrowing, CRC-32 */
-    uint32_t decode_launches, jump_launches;
+    double kernel_ms[7];    /* find (block starts and probes), decode, stored copies, span-local resolution,
+                               span windows and bytes, the next segment's window, CRC-32 */
+    uint32_t decode_launches, reserved;
     uint64_t in_bytes;      /* compressed bytes uploaded, all segments */
     uint64_t out_bytes;     /* bytes produced */
     uint64_t jobs, extents, stored_blocks;
+    uint64_t probes;        /* probe points (resynchronization inside long blocks) */
 } gi_profile;
 
 GI_API int gi_last_profile(const gi_ctx* ctx, gi_profile* profile);
