@@ -29,6 +29,7 @@ EXPORTED = (
     "gi_inflate_device",
     "gi_inflate_gzip",
     "gi_last_profile",
+    "gi_crc32_device_noalloc",
 )
 
 
@@ -112,6 +113,8 @@ def load(path=None):
     lib.gi_inflate_gzip.restype = ctypes.c_int
     lib.gi_last_profile.argtypes = [vp, ctypes.POINTER(Profile)]
     lib.gi_last_profile.restype = ctypes.c_int
+    lib.gi_crc32_device_noalloc.argtypes = [ctypes.c_int, vp, u64, vp, vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.gi_crc32_device_noalloc.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -225,3 +228,15 @@ class Gpu:
 
     def last_isize(self):
         return self.lib.gi_last_isize(self.ctx)
+
+
+def crc32_device_noalloc(d_data, size, d_crc, device=0, stream=None):
+    """CRC-32 of `size` bytes at device pointer d_data into the uint32 at device pointer d_crc,
+    through the entry point that allocates nothing (gi_crc32_device_noalloc). Asynchronous on
+    `stream` (a raw cudaStream_t value, or None for the default stream)."""
+    lib = load()
+    err = ctypes.create_string_buffer(256)
+    rc = lib.gi_crc32_device_noalloc(device, ctypes.c_void_p(d_data), size, ctypes.c_void_p(d_crc),
+                                     ctypes.c_void_p(stream) if stream else None, err, 256)
+    if rc != GI_OK:
+        raise InflateError(rc, err.value.decode(errors="replace"))

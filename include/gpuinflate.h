@@ -132,6 +132,17 @@ typedef struct {
 
 GI_API int gi_last_profile(const gi_ctx* ctx, gi_profile* profile);
 
+/* CRC-32 (gzip's) of size bytes already in GPU memory on `device`, written to *d_crc (a device
+ * pointer), launched on `stream` (a cudaStream_t; NULL for the default stream) without waiting.
+ * For callers that cannot allocate device memory: it allocates nothing, its scratch is a fixed
+ * 1 MiB array that every GPU loading this library holds until the process exits. Limits: at
+ * most 1 GiB per call, d_data 16-byte aligned (else GI_ERR_ARG, with the reason in err). The
+ * first call on a device looks the array up, so make it before any stream capture on that
+ * device; calls that overlap on one device share the array and race. No counterpart in the
+ * reference (its CRC is computed on the host by its caller). */
+GI_API int gi_crc32_device_noalloc(int device, const void* d_data, uint64_t size, uint32_t* d_crc, void* stream,
+                                   char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif
