@@ -46,6 +46,18 @@ struct Code {  // canonical code data for codes longer than the lookup
     uint16_t offs[16];   // index of the first symbol of each length in syms
 };
 
+struct Job1 {
+    uint64_t stop;
+    uint64_t limit;     // min(stop, end_bit + 1): one comparison per symbol checks both
+    uint64_t end_bit;
+    uint64_t end_byte;
+    const Start* tg;
+    int t, tend;        // next target, end of the stream's targets
+    uint64_t tbit;      // targets[t].bit, or UINT64_MAX
+};
+
+// per-warp shared memory: the decoder's tables, and the state of its current job that the hot loop
+// does not touch (kept out of registers)
 struct __align__(16) Tables {
     uint32_t lit[1 << LB];
     uint32_t dist[1 << DB];
@@ -58,6 +70,8 @@ struct __align__(16) Tables {
     uint8_t clh[1 << CB];  // (length << 5) | symbol
     int32_t state;         // which tables are loaded: 0 none, 1 fixed, 2 dynamic
     uint32_t pad;
+    Job1 j;                // the job's limits and target cursor
+    JobResult r;           // the job's result, written as it goes
 };
 
 __device__ const uint16_t c_lbase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
@@ -357,15 +371,6 @@ __device__ __forceinline__ void emit_run(Out& o, uint32_t len, uint16_t v, int l
     o.op += len;
 }
 
-struct Job1 {
-    uint64_t stop;
-    uint64_t limit;     // min(stop, end_bit + 1): one comparison per symbol checks both
-    uint64_t end_bit;
-    uint64_t end_byte;
-    const Start* tg;
-    int t, tend;        // next target, end of the stream's targets
-    uint64_t tbit;      // targets[t].bit, or UINT64_MAX
-};
 
 // Starts a new extent for the decoder at `state`; false when the pool or the extent list is full.
 __device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, int job) {
@@ -467,7 +472,7 @@ __device__ void decode_job(Ctx& C, int k) {
     Tables& T = *C.T;
     const Job J = C.a.jobs[k];
     const StreamDesc S = C.a.streams[J.stream];
-    Job1 j;
+    Job1& j = T.j;
     j.stop = S.stop;
     j.end_bit = S.end_bit;
     j.end_byte = S.end_bit >> 3;
@@ -478,7 +483,7 @@ __device__ void decode_job(Ctx& C, int k) {
     j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
     const bool check_refs = (J.flags & JOB_CHECK_REFS) != 0;
 
-    JobResult r;
+    JobResult& r = T.r;
     r.eob_bit = UINT64_MAX;
     r.eob_out = 0;
     r.status = S_OK;
