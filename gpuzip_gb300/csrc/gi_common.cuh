@@ -156,12 +156,25 @@ int decode_blocks_per_sm();
 int launch_decode(const DecodeArgs& a, int grid, void* stream);
 int launch_probe(const ProbeArgs& a, int grid, void* stream);
 int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream);
-// the output is resolved in spans of this many positions (a multiple of 16 and at least WINDOW)
+// the output is resolved in spans of at most this many positions (a multiple of 16, at least WINDOW)
 constexpr uint64_t SPAN = 512 * 1024;
-// passes: 1 = local resolution (and the check for matches before the start), 2 = windows and bytes
-int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t total, uint32_t W,
-                   const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad, uint8_t* out, int passes,
-                   void* stream);
+// a span of output positions [start, end) of one stream; W: bytes of that stream before start that
+// the span may copy from (0 at the stream's start, at most WINDOW); start is a multiple of 16
+struct SpanDesc {
+    uint64_t start, end;
+    uint32_t W;
+    uint32_t stream;  // bad[stream] is set for a match before the stream's start
+};
+// passes: 1 = local resolution (and the check for matches before the start), 2 = windows and bytes.
+// One stream in spans of SPAN (the first with W bytes of seg_window before it):
+int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans, uint64_t nspans,
+                   uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad,
+                   uint8_t* out, int passes, void* stream);
+// Many streams (every stream starting at its first span, W 0); multi: (first span, span count) of
+// each stream with more than one span
+int launch_resolve_streams(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans,
+                           uint64_t nspans, const uint32_t* multi, uint32_t nmulti, uint16_t* out16, uint8_t* windows,
+                           int* bad, uint8_t* out, int passes, void* stream);
 int resolve_setup();  // once per device: kernel attributes (returns a cudaError_t)
 uint64_t resolve_map_slots(uint64_t seg_out_max);  // extra 16-bit slots out16 needs after the output
 int launch_next_window(const uint8_t* out, uint64_t total, const uint8_t* old, uint32_t W, uint8_t* nw, uint32_t newW,
@@ -169,6 +182,10 @@ int launch_next_window(const uint8_t* out, uint64_t total, const uint8_t* old, u
 int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
                 void* stream);
 uint64_t crc_scratch_words(uint64_t n);
+// CRC-32 of each of nstreams streams laid out as spans (stream s: spans first_span[s] .. + span_count[s])
+int launch_crc_streams(const uint8_t* data, const SpanDesc* spans, uint64_t nspans, uint32_t* span_crc,
+                       const uint32_t* first_span, const uint32_t* span_count, uint32_t nstreams, uint32_t* crc,
+                       void* stream);
 
 // host-side CRC-32 arithmetic (reflected polynomial 0xEDB88320)
 uint32_t crc32_combine_host(uint32_t crc1, uint32_t crc2, uint64_t len2);

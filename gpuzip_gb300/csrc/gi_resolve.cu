@@ -92,15 +92,16 @@ __device__ __forceinline__ int piece_of(const Piece* tp, int ntp, const Piece* _
 }
 
 __global__ void __launch_bounds__(R1_THREADS) k_local(const uint16_t* __restrict__ pool, const Piece* __restrict__ pieces,
-                                                      int npieces, uint64_t total, uint64_t span, uint32_t W,
+                                                      int npieces, const SpanDesc* __restrict__ spans, uint64_t nspans,
                                                       uint16_t* out16, int* bad) {
     __shared__ volatile uint16_t val[TILE];
     __shared__ volatile uint16_t ptr[TILE];
     __shared__ Piece tp[TILE_PIECES];
     __shared__ int ntp, pcur;
-    const uint64_t nspans = (total + span - 1) / span;
     for (uint64_t sp = blockIdx.x; sp < nspans; sp += gridDim.x) {
-        const uint64_t s0 = sp * span, s1 = s0 + span < total ? s0 + span : total;
+        const SpanDesc sd = spans[sp];
+        const uint64_t s0 = sd.start, s1 = sd.end;
+        const uint32_t W = sd.W;
         if (threadIdx.x == 0) {
             int lo = 0, hi = npieces - 1;  // the last piece with dst <= s0
             while (lo < hi) {
@@ -154,8 +155,8 @@ __global__ void __launch_bounds__(R1_THREADS) k_local(const uint16_t* __restrict
                 if (i < n && v[k] > REF) {
                     int64_t src = (int64_t)p - (int64_t)(v[k] - REF);
                     if (src < (int64_t)s0) {
-                        if (src < -(int64_t)W) {
-                            *bad = 1;  // a match before the stream's start
+                        if (src < (int64_t)s0 - (int64_t)W) {
+                            bad[sd.stream] = 1;  // a match before the stream's start
                             r[k] = 0;
                         } else {
                             r[k] = (uint16_t)(256 + (src - ((int64_t)s0 - (int64_t)WINDOW)));
@@ -313,32 +314,57 @@ __global__ void __launch_bounds__(WT) k_fill(const uint16_t* __restrict__ out16,
     }
 }
 
-// pass 3: bytes, 16 per thread
-__global__ void k_final(const uint16_t* __restrict__ out16, uint64_t total, uint64_t span,
+// pass 3: bytes, 16 per thread per step; a block per span (span starts are multiples of 16)
+__global__ void k_final(const uint16_t* __restrict__ out16, const SpanDesc* __restrict__ spans, uint64_t nspans,
                         const uint8_t* __restrict__ windows, uint8_t* __restrict__ out) {
-    uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * 16;
-    if (i >= total) return;
-    if (i + 16 <= total) {
-        const uint4* s = (const uint4*)(out16 + i);
-        uint4 a = s[0], b = s[1];
-        uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-        const uint8_t* win = windows + (i / span) * WINDOW;  // 16 positions never straddle a span
-        uint32_t q[4];
+    for (uint64_t sp = blockIdx.x; sp < nspans; sp += gridDim.x) {
+        const SpanDesc sd = spans[sp];
+        const uint8_t* win = windows + sp * WINDOW;
+        for (uint64_t i = sd.start + (uint64_t)threadIdx.x * 16; i < sd.end; i += (uint64_t)blockDim.x * 16) {
+            if (i + 16 <= sd.end) {
+                const uint4* src = (const uint4*)(out16 + i);
+                uint4 a = src[0], b = src[1];
+                uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+                uint32_t q[4];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            uint32_t lo = w[2 * k] & 0xffff, hi = w[2 * k] >> 16, lo2 = w[2 * k + 1] & 0xffff, hi2 = w[2 * k + 1] >> 16;
-            uint32_t b0 = lo < 256 ? lo : win[lo - 256];
-            uint32_t b1 = hi < 256 ? hi : win[hi - 256];
-            uint32_t b2 = lo2 < 256 ? lo2 : win[lo2 - 256];
-            uint32_t b3 = hi2 < 256 ? hi2 : win[hi2 - 256];
-            q[k] = b0 | b1 << 8 | b2 << 16 | b3 << 24;
+                for (int k = 0; k < 4; k++) {
+                    uint32_t lo = w[2 * k] & 0xffff, hi = w[2 * k] >> 16, lo2 = w[2 * k + 1] & 0xffff,
+                             hi2 = w[2 * k + 1] >> 16;
+                    uint32_t b0 = lo < 256 ? lo : win[lo - 256];
+                    uint32_t b1 = hi < 256 ? hi : win[hi - 256];
+                    uint32_t b2 = lo2 < 256 ? lo2 : win[lo2 - 256];
+                    uint32_t b3 = hi2 < 256 ? hi2 : win[hi2 - 256];
+                    q[k] = b0 | b1 << 8 | b2 << 16 | b3 << 24;
+                }
+                *(uint4*)(out + i) = make_uint4(q[0], q[1], q[2], q[3]);
+            } else {
+                for (uint64_t k = i; k < sd.end; k++) {
+                    uint32_t v = out16[k];
+                    out[k] = v < 256 ? (uint8_t)v : win[v - 256];
+                }
+            }
         }
-        *(uint4*)(out + i) = make_uint4(q[0], q[1], q[2], q[3]);
-    } else {
-        for (uint64_t k = i; k < total; k++) {
-            uint32_t v = out16[k];
-            out[k] = v < 256 ? (uint8_t)v : windows[(k / span) * WINDOW + v - 256];
+    }
+}
+
+// Entry windows of the spans of many streams (the batched form): a block per stream with more
+// than one span walks its spans in order; window[first] is not read (nothing reaches before a
+// stream's start without being invalid).
+__global__ void __launch_bounds__(WT) k_chain_streams(const uint16_t* __restrict__ out16,
+                                                      const SpanDesc* __restrict__ spans,
+                                                      const uint32_t* __restrict__ multi, uint32_t nmulti,
+                                                      uint8_t* __restrict__ windows) {
+    __shared__ __align__(16) uint8_t win[WINDOW];
+    for (uint32_t m = blockIdx.x; m < nmulti; m += gridDim.x) {
+        const uint32_t first = multi[2 * m], count = multi[2 * m + 1];
+        for (int j = threadIdx.x; j < (int)WINDOW; j += WT) win[j] = 0;
+        __syncthreads();
+        for (uint32_t s = first + 1; s < first + count; s++) {
+            uint16_t v[WPER];
+            load_map(out16 + spans[s - 1].end - WINDOW, v);
+            apply_map(v, win, windows + (uint64_t)s * WINDOW);
         }
+        __syncthreads();
     }
 }
 
@@ -451,6 +477,73 @@ __global__ void k_crc_tail(const uint8_t* data, uint64_t full_bytes, uint32_t ta
     *result = tail ? mulmod(a, x8tail) ^ c : a;
 }
 
+// CRC-32 of many streams (the batched form): a block per span computes the span's CRC from 32 lane
+// CRCs per 4 KiB step merged with x^(8n) multipliers for any n (square-and-multiply over the table
+// below), and a thread per stream merges its spans' CRCs in order.
+__constant__ uint32_t c_x8pow[48];  // x^(8 * 2^k) mod P
+
+__device__ uint32_t x8n_dev(uint64_t n) {
+    uint32_t p = 1u << 31;  // x^0
+    for (int k = 0; n; k++, n >>= 1)
+        if (n & 1) p = mulmod(p, c_x8pow[k]);
+    return p;
+}
+
+__device__ __forceinline__ uint32_t crc_combine_dev(uint32_t a, uint32_t b, uint64_t len_b) {
+    return len_b ? mulmod(a, x8n_dev(len_b)) ^ b : a;
+}
+
+__global__ void __launch_bounds__(256) k_crc_spans(const uint8_t* __restrict__ data, const SpanDesc* __restrict__ spans,
+                                                    uint64_t nspans, uint32_t* __restrict__ span_crc) {
+    __shared__ uint32_t table[256];
+    __shared__ uint32_t part[8];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        uint32_t c = (uint32_t)i;
+        for (int b = 0; b < 8; b++) c = c & 1 ? POLY ^ (c >> 1) : c >> 1;
+        table[i] = c;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint64_t sp = blockIdx.x; sp < nspans; sp += gridDim.x) {
+        const SpanDesc sd = spans[sp];
+        const uint64_t len = sd.end - sd.start;
+        // warp w: bytes [w * len / 8, (w + 1) * len / 8); lane slices of equal size within it
+        const uint64_t a = sd.start + w * len / 8, b = sd.start + (w + 1) * len / 8;
+        const uint64_t slice = (b - a + 31) / 32;
+        const uint64_t la = a + lane * slice < b ? a + lane * slice : b;
+        const uint64_t lb = la + slice < b ? la + slice : b;
+        uint32_t c = 0xffffffffu;
+        for (uint64_t i = la; i < lb; i++) c = table[(c ^ data[i]) & 255] ^ (c >> 8);
+        c = lb > la ? ~c : 0u;
+        // merge the lanes in order (lane 0 takes each next lane's CRC with its length)
+        uint32_t acc = 0;
+        for (int l = 0; l < 32; l++) {
+            uint32_t cl = __shfl_sync(0xffffffffu, c, l);
+            uint64_t ll = __shfl_sync(0xffffffffu, lb - la, l);
+            if (lane == 0) acc = crc_combine_dev(acc, cl, ll);
+        }
+        if (lane == 0) part[w] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int k = 0; k < 8; k++) t = crc_combine_dev(t, part[k], (k + 1) * len / 8 - k * len / 8);
+            span_crc[sp] = t;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_crc_streams(const SpanDesc* __restrict__ spans, const uint32_t* __restrict__ span_crc,
+                              const uint32_t* __restrict__ first_span, const uint32_t* __restrict__ span_count,
+                              uint32_t nstreams, uint32_t* __restrict__ crc) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nstreams) return;
+    uint32_t c = 0;
+    for (uint32_t k = first_span[s]; k < first_span[s] + span_count[s]; k++)
+        c = crc_combine_dev(c, span_crc[k], spans[k].end - spans[k].start);
+    crc[s] = c;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- host side
@@ -530,23 +623,22 @@ int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, i
     return 1;
 }
 
-int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, uint64_t total, uint32_t W,
-                   const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad, uint8_t* out, int passes,
-                   void* stream) {
+int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans, uint64_t nspans,
+                   uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad,
+                   uint8_t* out, int passes, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (!total || npieces <= 0) return 0;
-    uint64_t nspans = (total + SPAN - 1) / SPAN;
     int launches = 0;
+    int dev = 0, nsm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (passes & 1) {
-        int dev = 0, nsm = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         uint64_t grid = nspans < (uint64_t)nsm * 4 ? nspans : (uint64_t)nsm * 4;
-        k_local<<<(unsigned)grid, R1_THREADS, 0, st>>>(pool, pieces, npieces, total, SPAN, W, out16, bad);
+        k_local<<<(unsigned)grid, R1_THREADS, 0, st>>>(pool, pieces, npieces, spans, nspans, out16, bad);
         launches++;
     }
     if (passes & 2) {
-        // groups of L spans: L about sqrt(spans) balances the three phases
+        // one stream, spans of SPAN: groups of L spans, L about sqrt(spans) balances the three phases
         uint64_t L = 1;
         while (L * L < nspans) L++;
         uint64_t ngroups = (nspans + L - 1) / L;
@@ -558,14 +650,60 @@ int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, uint6
         }
         k_chain<<<1, WT, 0, st>>>(maps, ngroups, L, nspans, seg_window, W, windows);
         k_fill<<<(unsigned)ngroups, WT, 0, st>>>(out16, nspans, SPAN, L, windows);
-        k_final<<<blocks_for((total + 15) / 16, 256), 256, 0, st>>>(out16, total, SPAN, windows, out);
+        uint64_t fgrid = nspans < (uint64_t)nsm * 8 ? nspans : (uint64_t)nsm * 8;
+        k_final<<<(unsigned)fgrid, 256, 0, st>>>(out16, spans, nspans, windows, out);
         launches += 3;
     }
     return launches;
 }
 
+int launch_resolve_streams(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans,
+                           uint64_t nspans, const uint32_t* multi, uint32_t nmulti, uint16_t* out16, uint8_t* windows,
+                           int* bad, uint8_t* out, int passes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!nspans || npieces <= 0) return 0;
+    int launches = 0;
+    int dev = 0, nsm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (passes & 1) {
+        uint64_t grid = nspans < (uint64_t)nsm * 4 ? nspans : (uint64_t)nsm * 4;
+        k_local<<<(unsigned)grid, R1_THREADS, 0, st>>>(pool, pieces, npieces, spans, nspans, out16, bad);
+        launches++;
+    }
+    if (passes & 2) {
+        if (nmulti) {
+            k_chain_streams<<<nmulti < (uint32_t)nsm * 2 ? nmulti : (uint32_t)nsm * 2, WT, 0, st>>>(out16, spans, multi,
+                                                                                                  nmulti, windows);
+            launches++;
+        }
+        uint64_t fgrid = nspans < (uint64_t)nsm * 8 ? nspans : (uint64_t)nsm * 8;
+        k_final<<<(unsigned)fgrid, 256, 0, st>>>(out16, spans, nspans, windows, out);
+        launches++;
+    }
+    return launches;
+}
+
 int resolve_setup() {
+    uint32_t pw[48];
+    for (int k = 0; k < 48; k++) pw[k] = x8n_host(1ull << k);
+    cudaError_t e = cudaMemcpyToSymbol(c_x8pow, pw, sizeof pw);
+    if (e != cudaSuccess) return (int)e;
     return (int)cudaFuncSetAttribute(k_compose, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * WINDOW);
+}
+
+int launch_crc_streams(const uint8_t* data, const SpanDesc* spans, uint64_t nspans, uint32_t* span_crc,
+                       const uint32_t* first_span, const uint32_t* span_count, uint32_t nstreams, uint32_t* crc,
+                       void* stream) {
+    if (!nstreams) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    int launches = 0;
+    if (nspans) {
+        k_crc_spans<<<(unsigned)(nspans < 152 * 8 ? nspans : 152 * 8), 256, 0, st>>>(data, spans, nspans, span_crc);
+        launches++;
+    }
+    k_crc_streams<<<(nstreams + 255) / 256, 256, 0, st>>>(spans, span_crc, first_span, span_count, nstreams, crc);
+    return launches + 1;
 }
 
 // 16-bit slots after the segment's symbols that hold the composed maps (one per group)

@@ -30,7 +30,11 @@ EXPORTED = (
     "gi_inflate_gzip",
     "gi_last_profile",
     "gi_crc32_device_noalloc",
+    "gi_inflate_batch",
 )
+
+GI_STREAM_GZIP = 1
+GI_STREAM_CRC = 2
 
 
 class Config(ctypes.Structure):
@@ -65,6 +69,14 @@ class Profile(ctypes.Structure):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("size", "kernel_ms")}
         d["kernel_ms"] = dict(zip(self.KINDS, list(self.kernel_ms)))
         return d
+
+
+class Stream(ctypes.Structure):
+    """gi_stream (gpuinflate.h): one stream of a batch"""
+
+    _fields_ = [("in_", ctypes.c_void_p), ("in_size", ctypes.c_uint64), ("flags", ctypes.c_uint32),
+                ("expected_crc", ctypes.c_uint32), ("out_offset", ctypes.c_uint64), ("out_size", ctypes.c_uint64),
+                ("in_used", ctypes.c_uint64), ("crc32", ctypes.c_uint32), ("status", ctypes.c_int32)]
 
 
 SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t)
@@ -115,6 +127,8 @@ def load(path=None):
     lib.gi_last_profile.restype = ctypes.c_int
     lib.gi_crc32_device_noalloc.argtypes = [ctypes.c_int, vp, u64, vp, vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.gi_crc32_device_noalloc.restype = ctypes.c_int
+    lib.gi_inflate_batch.argtypes = [vp, ctypes.POINTER(Stream), ctypes.c_uint32, vp, u64, ctypes.POINTER(Stats)]
+    lib.gi_inflate_batch.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -214,6 +228,51 @@ class Gpu:
             if rc != GI_OK:
                 raise self._error(rc)
         return n.value, st
+
+    def inflate_batch(self, streams, out_cap=None, out=None):
+        """Decodes many streams together (gi_inflate_batch). streams: list of bytes (raw Deflate), or
+        of (bytes, flags[, expected_crc]). Returns (list of dicts with output/status/crc32/in_used,
+        Stats). `out` may be a preallocated writable buffer (e.g. pinned); else one is made."""
+        n = len(streams)
+        arr = (Stream * max(1, n))()
+        keep = []
+        total_in = 0
+        for i, sdesc in enumerate(streams):
+            data, flags, crc = (sdesc, 0, 0) if isinstance(sdesc, (bytes, bytearray, memoryview)) else (
+                tuple(sdesc) + (0,) * (3 - len(sdesc)))
+            b = ctypes.create_string_buffer(bytes(data), len(data)) if len(data) else ctypes.create_string_buffer(1)
+            keep.append(b)
+            arr[i].in_ = ctypes.cast(b, ctypes.c_void_p)
+            arr[i].in_size = len(data)
+            arr[i].flags = flags
+            arr[i].expected_crc = crc & 0xFFFFFFFF
+            total_in += len(data)
+        if out is None:
+            out_cap = out_cap if out_cap is not None else max(1 << 20, 8 * total_in + 64 * n + (16 << 20))
+            outbuf = ctypes.create_string_buffer(out_cap)
+            out_ptr = ctypes.cast(outbuf, ctypes.c_void_p)
+        else:
+            outbuf = out
+            out_cap = len(out) if out_cap is None else out_cap
+            out_ptr = ctypes.c_void_p(ctypes.addressof(ctypes.c_char.from_buffer(out)))
+        st = Stats()
+        with self._lock:
+            rc = self.lib.gi_inflate_batch(self.ctx, arr, n, out_ptr, out_cap, ctypes.byref(st))
+            if rc != GI_OK:
+                raise self._error(rc)
+        res = []
+        view = memoryview(outbuf) if out is not None else None
+        for i in range(n):
+            a = arr[i]
+            d = {"status": a.status, "out_size": a.out_size, "in_used": a.in_used, "crc32": a.crc32,
+                 "out_offset": a.out_offset}
+            if a.status == GI_OK:
+                if view is not None:
+                    d["output"] = bytes(view[a.out_offset:a.out_offset + a.out_size])
+                else:
+                    d["output"] = ctypes.string_at(ctypes.addressof(outbuf) + a.out_offset, a.out_size)
+            res.append(d)
+        return res, st
 
     def last_profile(self):
         p = Profile()

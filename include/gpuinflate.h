@@ -115,6 +115,32 @@ GI_API int gi_inflate_device(gi_ctx* ctx, const void* d_in, uint64_t in_size, vo
 GI_API int gi_inflate_gzip(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, gi_sink sink, void* user,
                            uint64_t* member_size, gi_stats* stats);
 
+/* The batched form: n independent streams decoded together, in as few passes over the GPU as the
+ * context's buffers allow (one launch of each kernel for all streams of a pass). Every stream's
+ * output goes to out + out_offset (16-byte aligned, in order), its CRC-32 is computed on the GPU.
+ * Returns GI_OK when the call ran; each stream has its own status (GI_ERR_SPACE when its output
+ * did not fit out_cap). No counterpart in the reference (one stream per gi_inflate call, a
+ * context serving one call at a time: gpuinflate/gpuinflate.h:8); it replaces gpuzip's
+ * per-member calls (src/gz.rs:154-264) and its nvCOMP batches for ZIP entries
+ * (src/extract.rs:458-597). */
+#define GI_STREAM_GZIP 1u /* `in` is a gzip member: header parsed, trailer CRC-32 and ISIZE checked */
+#define GI_STREAM_CRC 2u  /* expected_crc holds the output's CRC-32 (a ZIP entry): checked */
+
+typedef struct {
+    const uint8_t* in;     /* the stream (host memory) */
+    uint64_t in_size;
+    uint32_t flags;        /* GI_STREAM_GZIP, GI_STREAM_CRC */
+    uint32_t expected_crc;
+    uint64_t out_offset;   /* set: where its output starts in out */
+    uint64_t out_size;     /* set */
+    uint64_t in_used;      /* set: bytes of in the stream took (a gzip member: through its trailer) */
+    uint32_t crc32;        /* set: CRC-32 of its output */
+    int32_t status;        /* set: GI_OK or the error of this stream */
+} gi_stream;
+
+GI_API int gi_inflate_batch(gi_ctx* ctx, gi_stream* streams, uint32_t n, uint8_t* out, uint64_t out_cap,
+                            gi_stats* stats);
+
 /* Where the GPU time of the last call on ctx went, per kernel kind (CUDA events around every
  * launch on the context's stream), and what the call moved. No counterpart in the reference
  * (its gi_stats has only the five stage times, which part 1 keeps). */
