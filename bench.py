@@ -180,6 +180,106 @@ def run_reference(args, member, info, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def many_workload(seed, n, total):
+    """The many-streams workload (cached on local disk between runs)."""
+    import pickle
+
+    from gpuzip_gb300 import workloads as W
+
+    os.makedirs(CACHE, exist_ok=True)
+    path = os.path.join(CACHE, f"many_s{seed}_n{n}_t{int(total)}.pkl")
+    if os.path.exists(path):
+        with open(path, "rb") as f:
+            return pickle.load(f)
+    streams = W.many_streams(seed=seed, n=n, total=total)
+    with open(path + ".tmp", "wb") as f:
+        pickle.dump(streams, f, protocol=pickle.HIGHEST_PROTOCOL)
+    os.replace(path + ".tmp", path)
+    return streams
+
+
+def run_batch(args, ws, rank, local):
+    """Many streams of uneven sizes: one library call per stream (the reference's launch model)
+    against one gi_inflate_batch call for all of them."""
+    import torch
+
+    from gpuzip_gb300 import gpuinflate
+
+    torch.cuda.set_device(local)
+    streams = many_workload(args.seed if args.seed != 2 else 3, args.nstreams, args.batch_total)
+    total_out = sum(x["size"] for x in streams)
+    total_in = sum(len(x["data"]) for x in streams)
+    g = gpuinflate.Gpu(local, segment_out_mb=args.seg_out_mb)
+    lib = g.lib
+    n = len(streams)
+    arr = (gpuinflate.Stream * n)()
+    for i, x in enumerate(streams):
+        arr[i].in_ = ctypes.cast(ctypes.c_char_p(x["data"]), ctypes.c_void_p)
+        arr[i].in_size = len(x["data"])
+        arr[i].flags = gpuinflate.GI_STREAM_GZIP if x["gzip"] else gpuinflate.GI_STREAM_CRC
+        arr[i].expected_crc = x["crc"]
+    out_cap = total_out + 16 * n + (64 << 20)
+    out = torch.empty(out_cap, dtype=torch.uint8).pin_memory()
+    stats = gpuinflate.Stats()
+
+    def batched():
+        rc = lib.gi_inflate_batch(g.ctx, arr, n, ctypes.c_void_p(out.data_ptr()), out_cap, ctypes.byref(stats))
+        bad = [i for i in range(n) if arr[i].status != 0 or arr[i].out_size != streams[i]["size"]]
+        if rc != 0 or bad:
+            raise RuntimeError(f"batched decode failed: rc {rc}, {len(bad)} streams wrong, e.g. {bad[:3]}")
+
+    msize = ctypes.c_uint64(0)
+
+    def plain():
+        times = []
+        for i, x in enumerate(streams):
+            t = time.perf_counter()
+            if x["gzip"]:
+                rc = lib.gi_inflate_gzip(g.ctx, x["data"], len(x["data"]), gpuinflate.SINK(), None, ctypes.byref(msize),
+                                         ctypes.byref(stats))
+            else:
+                rc = lib.gi_inflate(g.ctx, x["data"], len(x["data"]), 0, gpuinflate.SINK(), None, ctypes.byref(stats))
+                if rc == 0 and lib.gi_last_crc32(g.ctx) != x["crc"]:
+                    rc = -1
+            times.append(time.perf_counter() - t)
+            if rc != 0:
+                raise RuntimeError(f"plain decode of stream {i} failed: {rc}")
+        return times
+
+    for _ in range(args.warmup):
+        batched()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batched()
+    tb = (time.perf_counter() - t0) / args.steps
+    prof = g.last_profile().as_dict()
+    passes = stats.segments
+    plain()  # warm
+    t0 = time.perf_counter()
+    ptimes = plain()
+    tp = time.perf_counter() - t0
+    q = sorted(ptimes)
+    pct = lambda p: q[min(len(q) - 1, int(p * len(q)))] * 1e3
+    line = {
+        "metric": f"decompressed GB/s, {n} streams of uneven sizes (gzip members and CRC-checked entries), batched form",
+        "value": round(total_out / tb / 1e9, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(tb * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"{n} streams, sizes log-uniform over [1 KiB, 64 MiB] scaled to {total_out} bytes "
+                               f"in total ({total_in} compressed), one content kind and level (1/6/9) each, half gzip "
+                               "members, half raw entries with a known CRC-32 (seed 3)",
+                   "io": "host memory in, pinned host buffer out, CRC-32 of every stream computed on the GPU"},
+        "plain": {"value": round(total_out / tp / 1e9, 3), "unit": "GB/s", "calls": n,
+                  "call_ms_p50": round(pct(0.50), 3), "call_ms_p99": round(pct(0.99), 3),
+                  "call_ms_p999": round(pct(0.999), 3)},
+        "batched_over_plain": round(tp / tb, 2),
+        "batched_passes": passes, "gpu_launches": prof["launches"],
+        "stages_ms": {k: round(v, 2) for k, v in prof["kernel_ms"].items()},
+    }
+    print(json.dumps(line), flush=True)
+    g.close()
+
+
 def config_of(args, info):
     return {"workload": f"one gzip member, {args.nseg} x 1 MiB segments of mixed content (seed {args.seed}), levels 1/6/9 "
                         "in one Deflate stream",
@@ -200,8 +300,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="one device-resident decode, no timing (for ncu)")
+    ap.add_argument("--workload", default="member", choices=["member", "batch"])
+    ap.add_argument("--nstreams", type=int, default=10000)
+    ap.add_argument("--batch-total", type=float, default=8e9)
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "batch":
+        run_batch(args, ws, rank, local)
+        return
     member, info = workload(args.seed, args.nseg)
     if args.impl == "reference":
         run_reference(args, member, info, ws, rank)

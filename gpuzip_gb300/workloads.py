@@ -311,3 +311,59 @@ def mutate(data, rng):
             n = min(1 + rng.below(4096), len(m) - a, len(m) - b)
             m[b : b + n] = m[a : a + n]
     return bytes(m)
+
+
+# ---------------------------------------------------------------- many streams (batched, served)
+
+
+def stream_content(seed, index, size, kind):
+    """`size` bytes of one content kind (the mixed workload's four), seeded by (seed, index)."""
+    rng = np.random.default_rng([seed, 3, index])
+    if kind == KIND_TEXT:
+        return log_text(int(rng.integers(1 << 62)), size, exact=True, vocab_seed=seed) if size else b""
+    if kind == KIND_RANDOM:
+        return rng.integers(0, 256, size=size, dtype=np.uint8).tobytes()
+    if kind == KIND_PATTERN:
+        p = int(rng.integers(4, 65))
+        pat = rng.integers(0, 256, size=p, dtype=np.uint8)
+        a = np.tile(pat, size // p + 1)[:size]
+        nflip = size // 100
+        if nflip:
+            a[rng.integers(0, size, size=nflip)] = rng.integers(0, 256, size=nflip, dtype=np.uint8)
+        return a.tobytes()
+    start = int(rng.integers(0, 1 << 32))
+    vals = (start + np.cumsum(rng.integers(0, 16, size=(size + 3) // 4, dtype=np.uint64))) & 0xFFFFFFFF
+    return vals.astype("<u4").tobytes()[:size]
+
+
+def _stream_job(args):
+    seed, index, size, kind, level, gz = args
+    data = stream_content(seed, index, size, kind)
+    body = raw_deflate(data, int(level))
+    crc = zlib.crc32(data)
+    return index, (gzip_wrap(body, crc, len(data)) if gz else body), crc, len(data)
+
+
+def many_streams(seed=3, n=10000, lo=1 << 10, hi=64 << 20, total=None, workers=None):
+    """n independent streams: sizes log-uniform over [lo, hi] (then scaled so their sum is `total`
+    bytes when given), content of one kind each (p = 0.5/0.2/0.15/0.15 as the mixed workload),
+    level from {1, 6, 9}; even indices are gzip members, odd ones raw Deflate entries whose CRC-32
+    is known (as a ZIP entry's). Returns a list of dicts: data, gzip, crc, size."""
+    rng = np.random.default_rng([seed, 4])
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n))
+    if total:
+        sizes *= total / sizes.sum()
+    sizes = np.maximum(sizes.astype(np.int64), 1)
+    kinds = rng.choice(4, size=n, p=[0.5, 0.2, 0.15, 0.15])
+    levels = rng.choice(np.array([1, 6, 9]), size=n)
+    jobs = [(seed, i, int(sizes[i]), int(kinds[i]), int(levels[i]), i % 2 == 0) for i in range(n)]
+    # largest first, so the pool's workers end together
+    jobs.sort(key=lambda j: -j[2])
+    workers = workers or min(mp.cpu_count(), 32)
+    if n >= 16 and workers > 1:
+        with mp.get_context("spawn").Pool(workers) as pool:
+            res = pool.map(_stream_job, jobs, chunksize=1)
+    else:
+        res = [_stream_job(j) for j in jobs]
+    res.sort(key=lambda r: r[0])
+    return [{"data": d, "gzip": i % 2 == 0, "crc": c, "size": s} for i, d, c, s in res]
