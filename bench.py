@@ -280,6 +280,181 @@ def run_batch(args, ws, rank, local):
     g.close()
 
 
+def serve_pool(seed, npool):
+    """The serving workload's request pool: npool gzip members, sizes log-uniform over
+    [4 KiB, 256 MiB], content and level as the mixed workload (cached on local disk)."""
+    import pickle
+
+    from gpuzip_gb300 import workloads as W
+
+    os.makedirs(CACHE, exist_ok=True)
+    path = os.path.join(CACHE, f"serve_s{seed}_n{npool}.pkl")
+    if os.path.exists(path):
+        with open(path, "rb") as f:
+            return pickle.load(f)
+    pool = W.many_streams(seed=seed, n=npool, lo=4 << 10, hi=256 << 20, all_gzip=True)
+    for j, x in enumerate(pool):
+        x["damaged"] = W.zero_sector(x["data"], seed, j)
+    with open(path + ".tmp", "wb") as f:
+        pickle.dump(pool, f, protocol=pickle.HIGHEST_PROTOCOL)
+    os.replace(path + ".tmp", path)
+    return pool
+
+
+def run_serve(args, ws, rank, local):
+    """The serving loop: requests arriving as a Poisson process, each one gzip member of the pool
+    (a tenth of them rescue requests, whose member has one zeroed 4 KiB sector), served by the
+    request server (gi_server_*: HBM-budget admission into a resident device arena, passes of the
+    batched form on `--workers` concurrent decode loops) and, on the same arrivals, by the plain
+    form (one gi_inflate_gzip call per request, in arrival order, one at a time). Each form is also
+    run saturated (every request queued at once) for its capacity."""
+    import queue
+
+    import torch
+
+    from gpuzip_gb300 import gpuinflate
+    from gpuzip_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    seed = args.seed if args.seed != 2 else 5
+    pool = serve_pool(seed, args.pool)
+    arrivals, member, rescue = W.serve_trace(seed=seed, rate=args.rate, seconds=args.serve_seconds, npool=len(pool))
+    n = len(arrivals)
+    # every pool member and its damaged copy in one pinned host buffer
+    blobs = []
+    for x in pool:
+        blobs += [x["data"], x["damaged"]]
+    offs, pos = [], 0
+    for b in blobs:
+        offs.append(pos)
+        pos += (len(b) + 4095) // 4096 * 4096
+    host = torch.empty(pos, dtype=torch.uint8).pin_memory()
+    hv = host.numpy()
+    import numpy as np
+
+    for b, o in zip(blobs, offs):
+        hv[o:o + len(b)] = np.frombuffer(b, dtype=np.uint8)
+    base_ptr = host.data_ptr()
+    req_ptr = [base_ptr + offs[2 * int(member[k]) + int(rescue[k])] for k in range(n)]
+    req_size = [len(blobs[2 * int(member[k]) + int(rescue[k])]) for k in range(n)]
+    want_size = [pool[int(member[k])]["size"] for k in range(n)]
+    want_crc = [pool[int(member[k])]["crc"] for k in range(n)]
+    good_out = sum(want_size[k] for k in range(n) if not rescue[k])
+    offered = sum(want_size) / args.serve_seconds
+
+    def check(status, crc, size, k):
+        if rescue[k]:
+            return status != 0  # a damaged member must be refused
+        return status == 0 and crc == want_crc[k] and size == want_size[k]
+
+    def pct(v, p):
+        q = sorted(v)
+        return round(q[min(len(q) - 1, int(p * len(q)))] * 1e3, 3)
+
+    def lat_summary(lat):
+        return {"p50": pct(lat, 0.50), "p99": pct(lat, 0.99), "p999": pct(lat, 0.999), "max": round(max(lat) * 1e3, 3)}
+
+    def served(saturate):
+        srv = gpuinflate.Server(local, workers=args.workers, hbm_budget=args.hbm_budget)
+        for k in range(min(8, n)):  # warm-up: first launches, first touch of the output buffers
+            srv.submit((req_ptr[k], req_size[k]), tag=1 << 40 | k)
+        srv.drain()
+        srv.results.clear()
+        st0 = srv.stats()
+        base = srv.clock() + 0.02
+        for k in range(n):
+            if not saturate:
+                d = base + arrivals[k] - srv.clock()
+                if d > 0:
+                    time.sleep(d)
+            srv.submit((req_ptr[k], req_size[k]), tag=k)
+        srv.drain()
+        st = srv.stats()
+        res = srv.results
+        bad = [k for k in range(n) if not check(res[k]["status"], res[k]["crc32"], res[k]["out_size"], k)]
+        t_arr = [base + (0.0 if saturate else arrivals[k]) for k in range(n)]
+        lat = [res[k]["t_done"] - t_arr[k] for k in range(n)]
+        span = max(res[k]["t_done"] for k in range(n)) - base
+        batch = [res[k]["pass_requests"] for k in range(n)]
+        srv.close()
+        for key in ("submitted", "completed", "failed", "passes", "alone", "overlapped", "in_bytes", "out_bytes"):
+            st[key] -= st0[key]
+        st["busy_s"] = round(st["busy_s"] - st0["busy_s"], 3)
+        return {"gbs": round(good_out / span / 1e9, 3), "seconds": round(span, 3), "latency_ms": lat_summary(lat),
+                "wrong": len(bad), "mean_requests_per_pass": round(statistics.mean(batch), 2), "server": st}
+
+    def plain(saturate):
+        g = gpuinflate.Gpu(local)
+        lib = g.lib
+        stats = gpuinflate.Stats()
+        msize = ctypes.c_uint64(0)
+        q = queue.Queue()
+        done = [None] * n
+        status = [None] * n
+
+        def one(k):
+            rc = lib.gi_inflate_gzip(g.ctx, ctypes.cast(req_ptr[k], ctypes.c_char_p), req_size[k], gpuinflate.SINK(),
+                                     None, ctypes.byref(msize), ctypes.byref(stats))
+            return rc, lib.gi_last_crc32(g.ctx), stats.out_size
+
+        for k in range(min(8, n)):
+            one(k)
+
+        def consumer():
+            while True:
+                k = q.get()
+                if k is None:
+                    return
+                rc, crc, size = one(k)
+                done[k] = time.perf_counter()
+                status[k] = (rc, crc, size)
+
+        th = threading.Thread(target=consumer)
+        th.start()
+        base = time.perf_counter() + 0.02
+        for k in range(n):
+            if not saturate:
+                d = base + arrivals[k] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+            q.put(k)
+        q.put(None)
+        th.join()
+        g.close()
+        bad = [k for k in range(n) if not check(status[k][0], status[k][1], status[k][2], k)]
+        lat = [done[k] - (base + (0.0 if saturate else arrivals[k])) for k in range(n)]
+        span = max(done) - base
+        return {"gbs": round(good_out / span / 1e9, 3), "seconds": round(span, 3), "latency_ms": lat_summary(lat),
+                "wrong": len(bad)}
+
+    with Clocks() as clocks:
+        s_live = served(False)
+    p_live = plain(False)
+    s_sat = served(True)
+    p_sat = plain(True)
+    line = {
+        "metric": f"served decode: decompressed GB/s and request latency, Poisson {args.rate:g} requests/s for "
+                  f"{args.serve_seconds:g} s, 1 GB300",
+        "value": s_live["gbs"], "unit": "GB/s", "n_gpus": ws, "steps": 1, "warmup": 1,
+        "ms_per_step": round(s_live["seconds"] * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"{n} requests (seed {seed}): gzip members drawn from a pool of {len(pool)}, sizes "
+                               "log-uniform over [4 KiB, 256 MiB], content and level as the mixed workload; "
+                               f"{int(rescue.sum())} rescue requests carry one zeroed 4 KiB sector",
+                   "offered_gbs": round(offered / 1e9, 3), "hbm_budget": args.hbm_budget, "workers": args.workers,
+                   "io": "pinned host memory in, pinned host buffers out; CRC-32 and ISIZE of every request checked on "
+                         "the GPU"},
+        "latency_ms": s_live["latency_ms"],
+        "served": s_live,
+        "plain": p_live,
+        "saturated": {"served_gbs": s_sat["gbs"], "plain_gbs": p_sat["gbs"],
+                      "served_over_plain": round(s_sat["gbs"] / p_sat["gbs"], 2), "served": s_sat, "plain": p_sat},
+        "rescue": "not built: the damaged members of rescue requests are refused (GI_ERR_DATA), as gpuzip's test does",
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def config_of(args, info):
     return {"workload": f"one gzip member, {args.nseg} x 1 MiB segments of mixed content (seed {args.seed}), levels 1/6/9 "
                         "in one Deflate stream",
@@ -300,11 +475,19 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="one device-resident decode, no timing (for ncu)")
-    ap.add_argument("--workload", default="member", choices=["member", "batch"])
+    ap.add_argument("--workload", default="member", choices=["member", "batch", "serve"])
     ap.add_argument("--nstreams", type=int, default=10000)
     ap.add_argument("--batch-total", type=float, default=8e9)
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--pool", type=int, default=256, help="serve: distinct members requests draw from")
+    ap.add_argument("--workers", type=int, default=2, help="serve: concurrent decode loops")
+    ap.add_argument("--hbm-budget", type=float, default=120e9)
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "serve":
+        run_serve(args, ws, rank, local)
+        return
     if args.workload == "batch":
         run_batch(args, ws, rank, local)
         return

@@ -170,11 +170,31 @@ struct SpanDesc {
 int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans, uint64_t nspans,
                    uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad,
                    uint8_t* out, int passes, void* stream);
-// Many streams (every stream starting at its first span, W 0); multi: (first span, span count) of
-// each stream with more than one span
+// Many streams (every stream starting at its first span, W 0). A stream of fewer than
+// GROUPED_SPANS spans (but more than one) is listed in multi as (first span, span count); a longer
+// one is cut into groups of consecutive spans (about the square root of its span count each),
+// listed in groups, and its entry in grouped gives its first group and group count.
+constexpr uint32_t GROUPED_SPANS = 16;
+struct SpanGroup {
+    uint32_t first_span, count;
+    uint32_t map;  // slot of the group's composed map in `maps` (unused for a stream's last group)
+    uint32_t pad;
+};
+struct GroupedStream {
+    uint32_t first_group, ngroups;
+};
+struct StreamWindows {
+    const uint32_t* multi;
+    uint32_t nmulti;
+    const SpanGroup* groups;
+    uint32_t ngroups;
+    const GroupedStream* grouped;
+    uint32_t ngrouped;
+    uint16_t* maps;  // WINDOW 16-bit slots per composed map
+};
 int launch_resolve_streams(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans,
-                           uint64_t nspans, const uint32_t* multi, uint32_t nmulti, uint16_t* out16, uint8_t* windows,
-                           int* bad, uint8_t* out, int passes, void* stream);
+                           uint64_t nspans, const StreamWindows& sw, uint16_t* out16, uint8_t* windows, int* bad,
+                           uint8_t* out, int passes, void* stream);
 int resolve_setup();  // once per device: kernel attributes (returns a cudaError_t)
 uint64_t resolve_map_slots(uint64_t seg_out_max);  // extra 16-bit slots out16 needs after the output
 int launch_next_window(const uint8_t* out, uint64_t total, const uint8_t* old, uint32_t W, uint8_t* nw, uint32_t newW,

@@ -368,6 +368,78 @@ __global__ void __launch_bounds__(WT) k_chain_streams(const uint16_t* __restrict
     }
 }
 
+// The same scan per long stream of the batched form (groups never cross streams): the composed
+// map of every group but each stream's last, then a block per stream walks its groups, then a
+// block per group fills the windows inside it. A span's map is the last WINDOW values of the span.
+__global__ void __launch_bounds__(WT) k_compose_groups(const uint16_t* __restrict__ out16,
+                                                       const SpanDesc* __restrict__ spans,
+                                                       const SpanGroup* __restrict__ groups, uint32_t ngroups,
+                                                       uint16_t* __restrict__ maps) {
+    extern __shared__ __align__(16) uint16_t R[];
+    for (uint32_t gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
+        const SpanGroup gr = groups[gi];
+        if (gr.map == UINT32_MAX) continue;  // a stream's last group: its map is never used
+        uint16_t v[WPER];
+        load_map(out16 + spans[gr.first_span].end - WINDOW, v);
+#pragma unroll
+        for (int k = 0; k < WPER; k++) R[threadIdx.x * WPER + k] = v[k];
+        __syncthreads();
+        for (uint32_t s = gr.first_span + 1; s < gr.first_span + gr.count; s++) {
+            load_map(out16 + spans[s].end - WINDOW, v);
+#pragma unroll
+            for (int k = 0; k < WPER; k++) v[k] = v[k] < 256 ? v[k] : R[v[k] - 256];
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < WPER; k++) R[threadIdx.x * WPER + k] = v[k];
+            __syncthreads();
+        }
+        uint4* dst = (uint4*)(maps + (uint64_t)gr.map * WINDOW + threadIdx.x * WPER);
+        const uint4* srcv = (const uint4*)(R + threadIdx.x * WPER);
+#pragma unroll
+        for (int q = 0; q < 4; q++) dst[q] = srcv[q];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(WT) k_chain_groups(const SpanGroup* __restrict__ groups,
+                                                     const GroupedStream* __restrict__ grouped, uint32_t ngrouped,
+                                                     const uint16_t* __restrict__ maps, uint8_t* __restrict__ windows) {
+    __shared__ __align__(16) uint8_t win[WINDOW];
+    for (uint32_t m = blockIdx.x; m < ngrouped; m += gridDim.x) {
+        const GroupedStream gs = grouped[m];
+        uint8_t* w0 = windows + (uint64_t)groups[gs.first_group].first_span * WINDOW;
+        for (int j = threadIdx.x; j < (int)WINDOW; j += WT) win[j] = w0[j] = 0;
+        __syncthreads();
+        for (uint32_t g = gs.first_group; g + 1 < gs.first_group + gs.ngroups; g++) {
+            uint16_t v[WPER];
+            load_map(maps + (uint64_t)groups[g].map * WINDOW, v);
+            apply_map(v, win, windows + (uint64_t)groups[g + 1].first_span * WINDOW);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(WT) k_fill_groups(const uint16_t* __restrict__ out16,
+                                                    const SpanDesc* __restrict__ spans,
+                                                    const SpanGroup* __restrict__ groups, uint32_t ngroups,
+                                                    uint8_t* __restrict__ windows) {
+    __shared__ __align__(16) uint8_t win[WINDOW];
+    for (uint32_t gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
+        const SpanGroup gr = groups[gi];
+        const uint4* src = (const uint4*)(windows + (uint64_t)gr.first_span * WINDOW + threadIdx.x * WPER);
+        uint4* ws = (uint4*)(win + threadIdx.x * WPER);
+        ws[0] = src[0];
+        ws[1] = src[1];
+        __syncthreads();
+        for (uint32_t s = gr.first_span + 1; s < gr.first_span + gr.count; s++) {
+            uint16_t v[WPER];
+            load_map(out16 + spans[s - 1].end - WINDOW, v);
+            apply_map(v, win, windows + (uint64_t)s * WINDOW);
+        }
+        __syncthreads();
+    }
+}
+
 // the window for the next segment: the last 32 KiB of (old window ++ this segment's output)
 __global__ void k_next_window(const uint8_t* __restrict__ out, uint64_t total, const uint8_t* __restrict__ old,
                               uint32_t W, uint8_t* __restrict__ nw, uint32_t newW) {
@@ -477,9 +549,9 @@ __global__ void k_crc_tail(const uint8_t* data, uint64_t full_bytes, uint32_t ta
     *result = tail ? mulmod(a, x8tail) ^ c : a;
 }
 
-// CRC-32 of many streams (the batched form): a block per span computes the span's CRC from 32 lane
-// CRCs per 4 KiB step merged with x^(8n) multipliers for any n (square-and-multiply over the table
-// below), and a thread per stream merges its spans' CRCs in order.
+// CRC-32 of many streams (the batched form): span CRCs (k_crc_spans), then stream CRCs
+// (k_crc_streams); lengths that are not a constant of the launch take x^(8n) by square-and-multiply
+// over the table below.
 __constant__ uint32_t c_x8pow[48];  // x^(8 * 2^k) mod P
 
 __device__ uint32_t x8n_dev(uint64_t n) {
@@ -493,10 +565,15 @@ __device__ __forceinline__ uint32_t crc_combine_dev(uint32_t a, uint32_t b, uint
     return len_b ? mulmod(a, x8n_dev(len_b)) ^ b : a;
 }
 
+// CRC-32 of every span of the batched form: a block per span, whose warps take the span's 4 KiB
+// tiles in turn (32 lanes x 128 contiguous bytes, merged with constant multipliers, as
+// k_crc_tiles), a partial last tile lane by lane with x^(8n) for its lengths; thread 0 then merges
+// the tile CRCs in order (x^(8*4096) for every full tile).
 __global__ void __launch_bounds__(256) k_crc_spans(const uint8_t* __restrict__ data, const SpanDesc* __restrict__ spans,
-                                                    uint64_t nspans, uint32_t* __restrict__ span_crc) {
+                                                    uint64_t nspans, uint32_t* __restrict__ span_crc, CrcConsts k,
+                                                    uint32_t x4096) {
     __shared__ uint32_t table[256];
-    __shared__ uint32_t part[8];
+    __shared__ uint32_t tcrc[SPAN / 4096];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
         uint32_t c = (uint32_t)i;
         for (int b = 0; b < 8; b++) c = c & 1 ? POLY ^ (c >> 1) : c >> 1;
@@ -506,41 +583,69 @@ __global__ void __launch_bounds__(256) k_crc_spans(const uint8_t* __restrict__ d
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint64_t sp = blockIdx.x; sp < nspans; sp += gridDim.x) {
         const SpanDesc sd = spans[sp];
-        const uint64_t len = sd.end - sd.start;
-        // warp w: bytes [w * len / 8, (w + 1) * len / 8); lane slices of equal size within it
-        const uint64_t a = sd.start + w * len / 8, b = sd.start + (w + 1) * len / 8;
-        const uint64_t slice = (b - a + 31) / 32;
-        const uint64_t la = a + lane * slice < b ? a + lane * slice : b;
-        const uint64_t lb = la + slice < b ? la + slice : b;
-        uint32_t c = 0xffffffffu;
-        for (uint64_t i = la; i < lb; i++) c = table[(c ^ data[i]) & 255] ^ (c >> 8);
-        c = lb > la ? ~c : 0u;
-        // merge the lanes in order (lane 0 takes each next lane's CRC with its length)
-        uint32_t acc = 0;
-        for (int l = 0; l < 32; l++) {
-            uint32_t cl = __shfl_sync(0xffffffffu, c, l);
-            uint64_t ll = __shfl_sync(0xffffffffu, lb - la, l);
-            if (lane == 0) acc = crc_combine_dev(acc, cl, ll);
+        const uint64_t len = sd.end - sd.start;  // at most SPAN; the start is 16-byte aligned
+        const uint32_t nfull = (uint32_t)(len / 4096), tail = (uint32_t)(len % 4096);
+        const uint32_t ntiles = nfull + (tail != 0);
+        for (uint32_t t = w; t < ntiles; t += 8) {
+            const uint8_t* base = data + sd.start + (uint64_t)t * 4096;
+            uint32_t c;
+            if (t < nfull) {
+                const uint4* p = (const uint4*)(base + lane * 128);
+                c = 0xffffffffu;
+#pragma unroll 2
+                for (int q = 0; q < 8; q++) {
+                    uint4 v = p[q];
+                    uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        c = table[(c ^ wv[j]) & 255] ^ (c >> 8);
+                        c = table[(c ^ (wv[j] >> 8)) & 255] ^ (c >> 8);
+                        c = table[(c ^ (wv[j] >> 16)) & 255] ^ (c >> 8);
+                        c = table[(c ^ (wv[j] >> 24)) & 255] ^ (c >> 8);
+                    }
+                }
+                c = ~c;
+#pragma unroll
+                for (int s = 0; s < 5; s++) {
+                    uint32_t other = __shfl_down_sync(0xffffffffu, c, 1 << s);
+                    if ((lane & ((2 << s) - 1)) == 0) c = mulmod(c, k.lane[s]) ^ other;
+                }
+            } else {
+                const uint32_t a = lane * 128 < tail ? lane * 128 : tail;
+                const uint32_t b = lane * 128 + 128 < tail ? lane * 128 + 128 : tail;
+                uint32_t cl = ~crc_bytes(table, base + a, (int)(b - a), 0xffffffffu);
+                if (b == a) cl = 0;
+                c = 0;
+                for (int l = 0; l < 32; l++) {
+                    uint32_t x = __shfl_sync(0xffffffffu, cl, l);
+                    uint32_t n = __shfl_sync(0xffffffffu, b - a, l);
+                    if (lane == 0) c = crc_combine_dev(c, x, n);
+                }
+            }
+            if (lane == 0) tcrc[t] = c;
         }
-        if (lane == 0) part[w] = acc;
         __syncthreads();
         if (threadIdx.x == 0) {
-            uint32_t t = 0;
-            for (int k = 0; k < 8; k++) t = crc_combine_dev(t, part[k], (k + 1) * len / 8 - k * len / 8);
-            span_crc[sp] = t;
+            uint32_t acc = 0;
+            for (uint32_t t = 0; t < nfull; t++) acc = mulmod(acc, x4096) ^ tcrc[t];
+            if (tail) acc = crc_combine_dev(acc, tcrc[nfull], tail);
+            span_crc[sp] = acc;
         }
         __syncthreads();
     }
 }
 
+// a thread per stream merges its spans' CRCs in order: every span but the last is SPAN bytes
 __global__ void k_crc_streams(const SpanDesc* __restrict__ spans, const uint32_t* __restrict__ span_crc,
                               const uint32_t* __restrict__ first_span, const uint32_t* __restrict__ span_count,
-                              uint32_t nstreams, uint32_t* __restrict__ crc) {
+                              uint32_t nstreams, uint32_t xspan, uint32_t* __restrict__ crc) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nstreams) return;
     uint32_t c = 0;
-    for (uint32_t k = first_span[s]; k < first_span[s] + span_count[s]; k++)
-        c = crc_combine_dev(c, span_crc[k], spans[k].end - spans[k].start);
+    for (uint32_t k = first_span[s]; k < first_span[s] + span_count[s]; k++) {
+        const uint64_t len = spans[k].end - spans[k].start;
+        c = len == SPAN ? mulmod(c, xspan) ^ span_crc[k] : crc_combine_dev(c, span_crc[k], len);
+    }
     crc[s] = c;
 }
 
@@ -658,8 +763,8 @@ int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const
 }
 
 int launch_resolve_streams(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans,
-                           uint64_t nspans, const uint32_t* multi, uint32_t nmulti, uint16_t* out16, uint8_t* windows,
-                           int* bad, uint8_t* out, int passes, void* stream) {
+                           uint64_t nspans, const StreamWindows& sw, uint16_t* out16, uint8_t* windows, int* bad,
+                           uint8_t* out, int passes, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (!nspans || npieces <= 0) return 0;
     int launches = 0;
@@ -672,10 +777,20 @@ int launch_resolve_streams(const uint16_t* pool, const Piece* pieces, int npiece
         launches++;
     }
     if (passes & 2) {
-        if (nmulti) {
-            k_chain_streams<<<nmulti < (uint32_t)nsm * 2 ? nmulti : (uint32_t)nsm * 2, WT, 0, st>>>(out16, spans, multi,
-                                                                                                  nmulti, windows);
+        const uint32_t cap = (uint32_t)nsm * 2;
+        if (sw.nmulti) {
+            k_chain_streams<<<sw.nmulti < cap ? sw.nmulti : cap, WT, 0, st>>>(out16, spans, sw.multi, sw.nmulti,
+                                                                              windows);
             launches++;
+        }
+        if (sw.ngrouped) {
+            k_compose_groups<<<sw.ngroups < cap ? sw.ngroups : cap, WT, 2 * WINDOW, st>>>(out16, spans, sw.groups,
+                                                                                         sw.ngroups, sw.maps);
+            k_chain_groups<<<sw.ngrouped < cap ? sw.ngrouped : cap, WT, 0, st>>>(sw.groups, sw.grouped, sw.ngrouped,
+                                                                                 sw.maps, windows);
+            k_fill_groups<<<sw.ngroups < cap ? sw.ngroups : cap, WT, 0, st>>>(out16, spans, sw.groups, sw.ngroups,
+                                                                             windows);
+            launches += 3;
         }
         uint64_t fgrid = nspans < (uint64_t)nsm * 8 ? nspans : (uint64_t)nsm * 8;
         k_final<<<(unsigned)fgrid, 256, 0, st>>>(out16, spans, nspans, windows, out);
@@ -689,7 +804,9 @@ int resolve_setup() {
     for (int k = 0; k < 48; k++) pw[k] = x8n_host(1ull << k);
     cudaError_t e = cudaMemcpyToSymbol(c_x8pow, pw, sizeof pw);
     if (e != cudaSuccess) return (int)e;
-    return (int)cudaFuncSetAttribute(k_compose, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * WINDOW);
+    e = cudaFuncSetAttribute(k_compose, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * WINDOW);
+    if (e != cudaSuccess) return (int)e;
+    return (int)cudaFuncSetAttribute(k_compose_groups, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * WINDOW);
 }
 
 int launch_crc_streams(const uint8_t* data, const SpanDesc* spans, uint64_t nspans, uint32_t* span_crc,
@@ -698,11 +815,15 @@ int launch_crc_streams(const uint8_t* data, const SpanDesc* spans, uint64_t nspa
     if (!nstreams) return 0;
     cudaStream_t st = (cudaStream_t)stream;
     int launches = 0;
+    CrcConsts k{};
+    for (int s = 0; s < 5; s++) k.lane[s] = x8n_host(128ull << s);
     if (nspans) {
-        k_crc_spans<<<(unsigned)(nspans < 152 * 8 ? nspans : 152 * 8), 256, 0, st>>>(data, spans, nspans, span_crc);
+        k_crc_spans<<<(unsigned)(nspans < 152 * 8 ? nspans : 152 * 8), 256, 0, st>>>(data, spans, nspans, span_crc, k,
+                                                                                     x8n_host(4096));
         launches++;
     }
-    k_crc_streams<<<(nstreams + 255) / 256, 256, 0, st>>>(spans, span_crc, first_span, span_count, nstreams, crc);
+    k_crc_streams<<<(nstreams + 255) / 256, 256, 0, st>>>(spans, span_crc, first_span, span_count, nstreams,
+                                                          x8n_host(SPAN), crc);
     return launches + 1;
 }
 

@@ -31,6 +31,12 @@ EXPORTED = (
     "gi_last_profile",
     "gi_crc32_device_noalloc",
     "gi_inflate_batch",
+    "gi_server_create",
+    "gi_server_submit",
+    "gi_server_drain",
+    "gi_server_clock",
+    "gi_server_read_stats",
+    "gi_server_destroy",
 )
 
 GI_STREAM_GZIP = 1
@@ -82,6 +88,42 @@ class Stream(ctypes.Structure):
 SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t)
 
 
+class ServerConfig(ctypes.Structure):
+    """gi_server_config (gpuinflate.h)"""
+
+    _fields_ = [("size", ctypes.c_uint32), ("device", ctypes.c_int32), ("workers", ctypes.c_uint32),
+                ("max_batch", ctypes.c_uint32), ("pass_out_mb", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("hbm_budget", ctypes.c_uint64), ("arena_bytes", ctypes.c_uint64)]
+
+
+class Result(ctypes.Structure):
+    """gi_result (gpuinflate.h): one finished request of the server"""
+
+    _fields_ = [("tag", ctypes.c_uint64), ("status", ctypes.c_int32), ("crc32", ctypes.c_uint32),
+                ("out_size", ctypes.c_uint64), ("in_used", ctypes.c_uint64), ("t_submit", ctypes.c_double),
+                ("t_admit", ctypes.c_double), ("t_start", ctypes.c_double), ("t_done", ctypes.c_double),
+                ("pass_requests", ctypes.c_uint32), ("worker", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerStats(ctypes.Structure):
+    """gi_server_stats (gpuinflate.h)"""
+
+    _fields_ = [("size", ctypes.c_uint32), ("workers", ctypes.c_uint32), ("submitted", ctypes.c_uint64),
+                ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("passes", ctypes.c_uint64),
+                ("alone", ctypes.c_uint64), ("overlapped", ctypes.c_uint64), ("in_bytes", ctypes.c_uint64),
+                ("out_bytes", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64), ("arena_bytes", ctypes.c_uint64),
+                ("arena_peak", ctypes.c_uint64), ("busy_s", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "size"}
+
+
+DONE = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(Result), ctypes.c_void_p)
+
+
 class InflateError(Exception):
     def __init__(self, code, msg):
         super().__init__(f"{['ok', 'data', 'truncated', 'aborted', 'gpu', 'arg', 'space'][code] if code < 7 else code}: {msg}")
@@ -129,6 +171,19 @@ def load(path=None):
     lib.gi_crc32_device_noalloc.restype = ctypes.c_int
     lib.gi_inflate_batch.argtypes = [vp, ctypes.POINTER(Stream), ctypes.c_uint32, vp, u64, ctypes.POINTER(Stats)]
     lib.gi_inflate_batch.restype = ctypes.c_int
+    lib.gi_server_create.argtypes = [ctypes.POINTER(ServerConfig), DONE, vp, ctypes.POINTER(vp), ctypes.c_char_p,
+                                     ctypes.c_size_t]
+    lib.gi_server_create.restype = ctypes.c_int
+    lib.gi_server_submit.argtypes = [vp, vp, u64, ctypes.c_uint32, ctypes.c_uint32, u64]
+    lib.gi_server_submit.restype = ctypes.c_int
+    lib.gi_server_drain.argtypes = [vp]
+    lib.gi_server_drain.restype = ctypes.c_int
+    lib.gi_server_clock.argtypes = [vp]
+    lib.gi_server_clock.restype = ctypes.c_double
+    lib.gi_server_read_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    lib.gi_server_read_stats.restype = ctypes.c_int
+    lib.gi_server_destroy.argtypes = [vp]
+    lib.gi_server_destroy.restype = None
     _lib = lib
     return lib
 
@@ -237,6 +292,7 @@ class Gpu:
         arr = (Stream * max(1, n))()
         keep = []
         total_in = 0
+        guess = 0  # output room: a gzip member's ISIZE, else 8 bytes per input byte
         for i, sdesc in enumerate(streams):
             data, flags, crc = (sdesc, 0, 0) if isinstance(sdesc, (bytes, bytearray, memoryview)) else (
                 tuple(sdesc) + (0,) * (3 - len(sdesc)))
@@ -247,8 +303,10 @@ class Gpu:
             arr[i].flags = flags
             arr[i].expected_crc = crc & 0xFFFFFFFF
             total_in += len(data)
+            isize = int.from_bytes(bytes(data[-4:]), "little") if (flags & GI_STREAM_GZIP) and len(data) >= 18 else -1
+            guess += isize if 0 <= isize <= 1032 * len(data) and isize > 8 * len(data) else 8 * len(data)
         if out is None:
-            out_cap = out_cap if out_cap is not None else max(1 << 20, 8 * total_in + 64 * n + (16 << 20))
+            out_cap = out_cap if out_cap is not None else max(1 << 20, guess + 64 * n + (16 << 20))
             outbuf = ctypes.create_string_buffer(out_cap)
             out_ptr = ctypes.cast(outbuf, ctypes.c_void_p)
         else:
@@ -299,3 +357,91 @@ def crc32_device_noalloc(d_data, size, d_crc, device=0, stream=None):
                                      ctypes.c_void_p(stream) if stream else None, err, 256)
     if rc != GI_OK:
         raise InflateError(rc, err.value.decode(errors="replace"))
+
+
+class Server:
+    """The request server (gi_server_*): requests are admitted into a device arena against an HBM
+    budget and decoded in passes of the batched form by `workers` loops whose passes overlap on
+    the GPU. Every finished request lands in ``results[tag]`` (a dict of gi_result's fields, plus
+    ``output`` when keep_output); on_done(result, data_ptr) is also called, from a server thread,
+    with the output valid only during that call."""
+
+    def __init__(self, device=0, workers=0, max_batch=0, pass_out_mb=0, hbm_budget=0, arena_bytes=0,
+                 keep_output=False, on_done=None, path=None):
+        self.lib = load(path)
+        self.results = {}
+        self._inputs = {}
+        self._lock = threading.Lock()
+        self._next = 0
+
+        def _cb(user, rp, data):
+            r = rp.contents
+            d = r.as_dict()
+            if keep_output and data and r.status == GI_OK:
+                d["output"] = ctypes.string_at(data, r.out_size)
+            if on_done is not None:
+                try:
+                    on_done(d, data)
+                except Exception:
+                    pass
+            with self._lock:
+                self._inputs.pop(r.tag, None)
+                self.results[r.tag] = d
+
+        self._cb = DONE(_cb)
+        cfg = ServerConfig(ctypes.sizeof(ServerConfig), device, workers, max_batch, pass_out_mb, 0, int(hbm_budget),
+                           int(arena_bytes))
+        srv = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(512)
+        rc = self.lib.gi_server_create(ctypes.byref(cfg), self._cb, None, ctypes.byref(srv), err, 512)
+        if rc != GI_OK:
+            raise InflateError(rc, f"server: {err.value.decode(errors='replace')}")
+        self.srv = srv
+
+    def submit(self, data, flags=GI_STREAM_GZIP, expected_crc=0, tag=None):
+        """Queues one request: bytes, or (host pointer, size) of memory the caller keeps alive until
+        its result arrives. Returns its tag."""
+        if isinstance(data, tuple):
+            ptr, size = data
+            keep = None
+        else:
+            keep = data if isinstance(data, bytes) else bytes(data)
+            ptr = ctypes.cast(ctypes.c_char_p(keep), ctypes.c_void_p).value
+            size = len(keep)
+        with self._lock:
+            if tag is None:
+                tag = self._next
+            self._next = max(self._next, tag) + 1
+            self._inputs[tag] = keep
+        rc = self.lib.gi_server_submit(self.srv, ctypes.c_void_p(ptr), size, flags, expected_crc & 0xFFFFFFFF, tag)
+        if rc != GI_OK:
+            with self._lock:
+                self._inputs.pop(tag, None)
+            raise InflateError(rc, "submit refused")
+        return tag
+
+    def drain(self):
+        self.lib.gi_server_drain(self.srv)
+
+    def clock(self):
+        """Seconds on the server's clock (the clock of every result's t_* fields)."""
+        return self.lib.gi_server_clock(self.srv)
+
+    def stats(self):
+        st = ServerStats()
+        st.size = ctypes.sizeof(ServerStats)
+        rc = self.lib.gi_server_read_stats(self.srv, ctypes.byref(st))
+        if rc != GI_OK:
+            raise InflateError(rc, "stats")
+        return st.as_dict()
+
+    def close(self):
+        if self.srv:
+            self.lib.gi_server_destroy(self.srv)
+            self.srv = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -344,11 +344,12 @@ def _stream_job(args):
     return index, (gzip_wrap(body, crc, len(data)) if gz else body), crc, len(data)
 
 
-def many_streams(seed=3, n=10000, lo=1 << 10, hi=64 << 20, total=None, workers=None):
+def many_streams(seed=3, n=10000, lo=1 << 10, hi=64 << 20, total=None, workers=None, all_gzip=False):
     """n independent streams: sizes log-uniform over [lo, hi] (then scaled so their sum is `total`
     bytes when given), content of one kind each (p = 0.5/0.2/0.15/0.15 as the mixed workload),
     level from {1, 6, 9}; even indices are gzip members, odd ones raw Deflate entries whose CRC-32
-    is known (as a ZIP entry's). Returns a list of dicts: data, gzip, crc, size."""
+    is known (as a ZIP entry's), or all gzip members with all_gzip. Returns a list of dicts: data,
+    gzip, crc, size."""
     rng = np.random.default_rng([seed, 4])
     sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n))
     if total:
@@ -356,7 +357,7 @@ def many_streams(seed=3, n=10000, lo=1 << 10, hi=64 << 20, total=None, workers=N
     sizes = np.maximum(sizes.astype(np.int64), 1)
     kinds = rng.choice(4, size=n, p=[0.5, 0.2, 0.15, 0.15])
     levels = rng.choice(np.array([1, 6, 9]), size=n)
-    jobs = [(seed, i, int(sizes[i]), int(kinds[i]), int(levels[i]), i % 2 == 0) for i in range(n)]
+    jobs = [(seed, i, int(sizes[i]), int(kinds[i]), int(levels[i]), all_gzip or i % 2 == 0) for i in range(n)]
     # largest first, so the pool's workers end together
     jobs.sort(key=lambda j: -j[2])
     workers = workers or min(mp.cpu_count(), 32)
@@ -366,4 +367,33 @@ def many_streams(seed=3, n=10000, lo=1 << 10, hi=64 << 20, total=None, workers=N
     else:
         res = [_stream_job(j) for j in jobs]
     res.sort(key=lambda r: r[0])
-    return [{"data": d, "gzip": i % 2 == 0, "crc": c, "size": s} for i, d, c, s in res]
+    return [{"data": d, "gzip": all_gzip or i % 2 == 0, "crc": c, "size": s} for i, d, c, s in res]
+
+
+def serve_trace(seed=5, rate=200.0, seconds=60.0, npool=256, rescue_frac=0.10):
+    """Arrivals of the serving workload: a Poisson process of `rate` requests per second for
+    `seconds`, each request drawing one member of a pool of `npool` (uniformly), a fraction
+    `rescue_frac` of them marked as rescue requests (their member arrives with one 4 KiB sector
+    zeroed). Returns (arrival times in seconds, pool index per request, rescue flag per request)."""
+    rng = np.random.default_rng([seed, 5])
+    n_guess = int(rate * seconds * 1.5) + 64
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n_guess))
+    while t[-1] < seconds:  # (practically never) more arrivals than the guess
+        t = np.concatenate([t, t[-1] + np.cumsum(rng.exponential(1.0 / rate, size=n_guess))])
+    t = t[t < seconds]
+    member = rng.integers(0, npool, size=len(t))
+    rescue = rng.random(len(t)) < rescue_frac
+    return t, member, rescue
+
+
+def zero_sector(member, seed, index):
+    """A copy of gzip member `member` with one 4 KiB sector (4 KiB-aligned in the file) zeroed
+    inside its compressed body (all of the body when it is shorter)."""
+    b = bytearray(member)
+    lo, hi = 10, max(11, len(b) - 8)
+    rng = np.random.default_rng([seed, 6, index])
+    first, last = lo // 4096, (hi - 1) // 4096
+    sec = int(rng.integers(first, last + 1))
+    a, e = max(lo, sec * 4096), min(hi, sec * 4096 + 4096)
+    b[a:e] = bytes(e - a)
+    return bytes(b)

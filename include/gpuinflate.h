@@ -169,6 +169,75 @@ GI_API int gi_last_profile(const gi_ctx* ctx, gi_profile* profile);
 GI_API int gi_crc32_device_noalloc(int device, const void* d_data, uint64_t size, uint32_t* d_crc, void* stream,
                                    char* err, size_t err_len);
 
+/* ------------------------------------------------------------------ part 3: the request server
+ *
+ * A request loop over the batched form, for a process that decodes many streams as they come
+ * (gpuzip's `test` and `extract` over a stream of archives). No counterpart in the reference,
+ * whose host decodes one member per gi_inflate call under a mutex (src/inflate.rs:60, :152).
+ *
+ * Requests are admitted against an HBM budget: a request's whole input is copied into a
+ * resident device arena as soon as the arena has room (in arrival order), so a pass never
+ * waits for its uploads. `workers` decode loops, each with its own stream and pass buffers,
+ * take every admitted request that fits their next pass when they become free; passes of
+ * different workers run on the GPU at the same time, so requests that arrive while a pass is
+ * running are decoded beside it, not after it. A request whose output cannot fit a pass is
+ * decoded on its own (segmented, from host memory). Results are delivered to a callback. */
+typedef struct gi_server gi_server;
+
+typedef struct {
+    uint32_t size;          /* sizeof(gi_server_config) (40) */
+    int32_t device;
+    uint32_t workers;       /* decode loops, i.e. passes that may run at once (0 = 2) */
+    uint32_t max_batch;     /* most requests in one pass (0 = 4096) */
+    uint32_t pass_out_mb;   /* output of one pass, MiB (0 = 2048, less when the budget is small) */
+    uint32_t reserved;
+    uint64_t hbm_budget;    /* device bytes the server may hold: pass buffers + arena (0 = 120 GB) */
+    uint64_t arena_bytes;   /* of which the input arena (0 = the rest of the budget, at most 64 GiB) */
+} gi_server_config;
+
+typedef struct {
+    uint64_t tag;           /* the caller's tag from gi_server_submit */
+    int32_t status;         /* GI_OK, or the error class of gi_inflate / gi_inflate_gzip */
+    uint32_t crc32;         /* CRC-32 of the output, computed on the GPU */
+    uint64_t out_size;
+    uint64_t in_used;       /* bytes of the input the stream took (gzip: through its trailer) */
+    double t_submit, t_admit, t_start, t_done;  /* seconds on the server's clock (gi_server_clock) */
+    uint32_t pass_requests; /* requests decoded in the same pass (1 for one decoded on its own) */
+    uint32_t worker;
+} gi_result;
+
+/* data: r->out_size bytes of output (NULL when status != GI_OK), valid only during the call.
+ * Called from a thread of the server, never two at once; it may call gi_server_submit, but not
+ * gi_server_drain or gi_server_destroy. */
+typedef void (*gi_done)(void* user, const gi_result* r, const uint8_t* data);
+
+typedef struct {
+    uint32_t size;          /* sizeof(gi_server_stats), set by the caller (104) */
+    uint32_t workers;
+    uint64_t submitted, completed, failed;
+    uint64_t passes;        /* passes run (a request decoded on its own counts as one) */
+    uint64_t alone;         /* requests decoded on their own */
+    uint64_t overlapped;    /* passes that started while another worker's pass was running */
+    uint64_t in_bytes, out_bytes;
+    uint64_t device_bytes;  /* device memory the server holds: pass buffers and arena */
+    uint64_t arena_bytes, arena_peak;  /* the input arena, and the most of it held at once */
+    double busy_s;          /* time during which at least one pass was running */
+} gi_server_stats;
+
+GI_API int gi_server_create(const gi_server_config* cfg, gi_done done, void* user, gi_server** server, char* err,
+                            size_t err_len);
+/* Queues one request; `in` (host memory) must stay valid until its callback has returned.
+ * flags: GI_STREAM_GZIP (one gzip member) or GI_STREAM_CRC (raw Deflate with a known CRC-32) or
+ * 0 (raw Deflate). Returns GI_OK, or GI_ERR_ARG (no input, or the server is shutting down). */
+GI_API int gi_server_submit(gi_server* server, const uint8_t* in, uint64_t in_size, uint32_t flags,
+                            uint32_t expected_crc, uint64_t tag);
+/* Waits until every submitted request has had its callback. */
+GI_API int gi_server_drain(gi_server* server);
+GI_API double gi_server_clock(const gi_server* server);
+GI_API int gi_server_read_stats(const gi_server* server, gi_server_stats* stats);
+/* Drains, stops the server's threads and frees its memory. */
+GI_API void gi_server_destroy(gi_server* server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,3 +60,33 @@ def test_bad_arguments_without_gpu(lib):
     assert lib.gi_last_error(None) == b"no context"
     assert lib.gi_device_name(None) == b""
     lib.gi_destroy(None)
+
+
+def test_server_struct_layouts():
+    assert ctypes.sizeof(gpuinflate.ServerConfig) == 40
+    assert ctypes.sizeof(gpuinflate.Result) == 72
+    assert ctypes.sizeof(gpuinflate.ServerStats) == 104
+    assert gpuinflate.Result.t_submit.offset == 32
+    assert gpuinflate.ServerStats.busy_s.offset == 96
+
+
+def test_server_bad_arguments_without_gpu(lib):
+    srv = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(512)
+    cb = gpuinflate.DONE(lambda user, r, data: None)
+    small = gpuinflate.ServerConfig(8)
+    assert lib.gi_server_create(ctypes.byref(small), cb, None, ctypes.byref(srv), err, 512) == gpuinflate.GI_ERR_ARG
+    assert b"too small" in err.value and srv.value is None
+    cfg = gpuinflate.ServerConfig(ctypes.sizeof(gpuinflate.ServerConfig))
+    assert lib.gi_server_create(ctypes.byref(cfg), gpuinflate.DONE(), None, ctypes.byref(srv), err, 512) == \
+        gpuinflate.GI_ERR_ARG
+    assert b"callback" in err.value
+    cfg.workers = 99
+    assert lib.gi_server_create(ctypes.byref(cfg), cb, None, ctypes.byref(srv), err, 512) == gpuinflate.GI_ERR_ARG
+    assert lib.gi_server_create(ctypes.byref(cfg), cb, None, None, err, 512) == gpuinflate.GI_ERR_ARG
+    assert lib.gi_server_submit(None, b"x", 1, 1, 0, 0) == gpuinflate.GI_ERR_ARG
+    assert lib.gi_server_drain(None) == gpuinflate.GI_ERR_ARG
+    st = gpuinflate.ServerStats(ctypes.sizeof(gpuinflate.ServerStats))
+    assert lib.gi_server_read_stats(None, ctypes.byref(st)) == gpuinflate.GI_ERR_ARG
+    assert lib.gi_server_clock(None) == 0.0
+    lib.gi_server_destroy(None)

@@ -93,3 +93,36 @@ def test_batch_output_space(gpu):
     res, _ = gpu.inflate_batch([s, s], out_cap=120_000)
     assert res[0]["status"] == 0
     assert res[1]["status"] == gpuinflate.GI_ERR_SPACE
+
+
+def test_batch_long_streams_scan_their_windows_in_groups(gpu):
+    # streams of 16 spans (8 MiB) and more take the grouped window scan; shorter ones the walk
+    items, wants = [], []
+    for i, n in enumerate((8 << 20, (8 << 20) + 12345, 21 << 20, 300_000, 35 << 20, 5000)):
+        text = W.log_text(70 + i, n, exact=True)
+        wants.append(text)
+        items.append((W.gzip_wrap(W.raw_deflate(text, [1, 6, 9][i % 3]), zlib.crc32(text), len(text)),
+                      gpuinflate.GI_STREAM_GZIP))
+    member, info = W.mixed_member(seed=8, nseg=24, seg_bytes=1 << 20, want_raw=False)
+    items.append((member, gpuinflate.GI_STREAM_GZIP))
+    wants.append(zlib.decompress(member, 31))
+    res, st = gpu.inflate_batch(items)
+    for i, (r, want) in enumerate(zip(res, wants)):
+        assert r["status"] == 0, i
+        assert r["out_size"] == len(want), i
+        assert r["output"] == want, i
+        assert r["crc32"] == zlib.crc32(want)
+
+
+def test_batch_high_ratio_members_in_one_pass(gpu):
+    # outputs hundreds of times their input: decoders sized from each member's ISIZE
+    items, wants = [], []
+    for i in range(6):
+        pat = bytes((i * 37 + k) & 255 for k in range(8 + 8 * i))
+        data = pat * ((24 << 20) // len(pat))
+        wants.append(data)
+        items.append((W.gzip_wrap(W.raw_deflate(data, 9), zlib.crc32(data), len(data)), gpuinflate.GI_STREAM_GZIP))
+    res, st = gpu.inflate_batch(items)
+    for i, (r, want) in enumerate(zip(res, wants)):
+        assert r["status"] == 0 and r["output"] == want, i
+    assert st.segments == 1
