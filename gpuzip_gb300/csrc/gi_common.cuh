@@ -164,12 +164,17 @@ struct SpanDesc {
     uint64_t start, end;
     uint32_t W;
     uint32_t stream;  // bad[stream] is set for a match before the stream's start
+    uint32_t piece0;  // the pieces that overlap the span: piece0 .. piece0 + npiece - 1
+    uint32_t npiece;
 };
+// fills piece0/npiece of every span (spans and pieces both sorted, the pieces back to back)
+void span_pieces(SpanDesc* spans, uint64_t nspans, const Piece* pieces, uint64_t npieces);
 // passes: 1 = local resolution (and the check for matches before the start), 2 = windows and bytes.
 // One stream in spans of SPAN (the first with W bytes of seg_window before it):
+// work: one word of device memory the launch uses as the span queue of k_local
 int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans, uint64_t nspans,
                    uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad,
-                   uint8_t* out, int passes, void* stream);
+                   uint8_t* out, int passes, unsigned* work, void* stream);
 // Many streams (every stream starting at its first span, W 0). A stream of fewer than
 // GROUPED_SPANS spans (but more than one) is listed in multi as (first span, span count); a longer
 // one is cut into groups of consecutive spans (about the square root of its span count each),
@@ -194,7 +199,7 @@ struct StreamWindows {
 };
 int launch_resolve_streams(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans,
                            uint64_t nspans, const StreamWindows& sw, uint16_t* out16, uint8_t* windows, int* bad,
-                           uint8_t* out, int passes, void* stream);
+                           uint8_t* out, int passes, unsigned* work, void* stream);
 int resolve_setup();  // once per device: kernel attributes (returns a cudaError_t)
 uint64_t resolve_map_slots(uint64_t seg_out_max);  // extra 16-bit slots out16 needs after the output
 int launch_next_window(const uint8_t* out, uint64_t total, const uint8_t* old, uint32_t W, uint8_t* nw, uint32_t newW,

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "gi_common.cuh"
+#include "gi_find_cl.h"
 
 namespace gz {
 namespace {
@@ -159,20 +160,6 @@ __device__ bool verify_header(const uint32_t* w, uint64_t end_word, uint64_t end
     return b.pos() <= end_bit;
 }
 
-// code-length code complete, from the 128 bits at a candidate whose first 17 bits passed
-__device__ __forceinline__ bool cl_code_complete(uint64_t v1, uint64_t v2) {
-    int hclen = (int)((v1 >> 13) & 15) + 4;
-    uint64_t f = (v1 >> 17) | (v2 << 47);
-    uint32_t sum = 0;
-#pragma unroll
-    for (int i = 0; i < 19; i++) {
-        uint32_t l = (uint32_t)(f >> (3 * i)) & 7;
-        uint32_t add = (uint32_t)(0x0102040810204000ull >> (8 * l)) & 0xff;  // 128 >> l, 0 for l = 0
-        sum += i < hclen ? add : 0;
-    }
-    return sum == 128;
-}
-
 // Candidates that pass the cheap tests queue up in bit order in the warp's shared-memory list and
 // are verified 32 at a time (one per lane), so the expensive check runs on full warps; the list
 // is drained whenever it holds a full batch, and the first batch with a pass gives the chunk's
@@ -186,6 +173,9 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
                                                           uint64_t* __restrict__ first,
                                                           const uint8_t* __restrict__ skip) {
     __shared__ uint32_t cand[FIND_WARPS][LIST];  // candidate bit, relative to the chunk's first word
+    __shared__ uint16_t cl4[CL4_ENTRIES];         // Kraft contributions of four code-length fields
+    for (int i = threadIdx.x; i < CL4_ENTRIES; i += blockDim.x) cl4[i] = cl4_entry((uint32_t)i);
+    __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint32_t* list = cand[wib];
     const uint64_t nwarps = (uint64_t)gridDim.x * FIND_WARPS;
@@ -242,7 +232,7 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
                         mm &= mm - 1;
                         uint64_t v1 = o ? (lo64 >> o) | (hi64 << (64 - o)) : lo64;
                         uint64_t v2 = hi64 >> o;
-                        if (cl_code_complete(v1, v2)) keep |= 1u << o;
+                        if (cl_complete_tab(v1, v2, cl4)) keep |= 1u << o;
                     }
                     mask = keep;
                 }

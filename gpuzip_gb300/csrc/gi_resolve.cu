@@ -68,116 +68,85 @@ constexpr int TILE = 2048;  // positions per tile: 4 per thread
 constexpr int TPT = TILE / R1_THREADS;
 constexpr uint16_t PENDING = 0xFFFF;
 
-// pass 1: every span resolved on its own (see the file comment). Thread t owns positions
-// 4t..4t+3 of a tile, so its four symbols come from one piece (almost always) and leave in one
-// 8-byte store; the pieces a tile touches are staged in shared memory.
-constexpr int TILE_PIECES = 64;
+// pass 1: every span resolved on its own (see the file comment). Position i of a tile belongs to
+// thread i % R1_THREADS (consecutive threads, consecutive positions: coalesced loads and stores,
+// no shared-memory bank conflicts). The span's pieces are staged in shared memory once, by all
+// threads, when there are at most SPAN_PIECES of them (else each thread searches the span's range
+// of the global list). Blocks take spans from a queue (`work`, zero at launch).
+constexpr int SPAN_PIECES = 512;
 
-__device__ __forceinline__ int piece_of(const Piece* tp, int ntp, const Piece* __restrict__ pieces, int npieces,
-                                        uint64_t p) {
-    // in the staged list (ntp > 0), else the global list by binary search; returns the index into the
-    // list searched (staged index when ntp > 0)
-    if (ntp > 0) {
-        int j = 0;
-        while (j + 1 < ntp && p >= tp[j + 1].dst) j++;
-        return j;
-    }
-    int lo = 0, hi = npieces - 1;
+// the piece holding position p among list[0 .. n) (sorted, back to back, list[0].dst <= p)
+__device__ __forceinline__ int piece_at(const Piece* list, int n, uint64_t p) {
+    int lo = 0, hi = n - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        if (pieces[mid].dst <= p) lo = mid;
+        if (list[mid].dst <= p) lo = mid;
         else hi = mid - 1;
     }
     return lo;
 }
 
-__global__ void __launch_bounds__(R1_THREADS) k_local(const uint16_t* __restrict__ pool, const Piece* __restrict__ pieces,
-                                                      int npieces, const SpanDesc* __restrict__ spans, uint64_t nspans,
-                                                      uint16_t* out16, int* bad) {
-    __shared__ volatile uint16_t val[TILE];
-    __shared__ volatile uint16_t ptr[TILE];
-    __shared__ Piece tp[TILE_PIECES];
-    __shared__ int ntp, pcur;
-    for (uint64_t sp = blockIdx.x; sp < nspans; sp += gridDim.x) {
+__global__ void __launch_bounds__(R1_THREADS, 4) k_local(const uint16_t* __restrict__ pool,
+                                                         const Piece* __restrict__ pieces, int npieces,
+                                                         const SpanDesc* __restrict__ spans, uint64_t nspans,
+                                                         uint16_t* out16, int* bad, unsigned* work) {
+    __shared__ uint16_t val[TILE];
+    __shared__ uint16_t ptr[TILE];
+    __shared__ Piece sp_pieces[SPAN_PIECES];
+    __shared__ unsigned next_span;
+    (void)npieces;
+    uint64_t sp = blockIdx.x;
+    while (sp < nspans) {
         const SpanDesc sd = spans[sp];
         const uint64_t s0 = sd.start, s1 = sd.end;
-        const uint32_t W = sd.W;
-        if (threadIdx.x == 0) {
-            int lo = 0, hi = npieces - 1;  // the last piece with dst <= s0
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (pieces[mid].dst <= s0) lo = mid;
-                else hi = mid - 1;
-            }
-            pcur = lo;
-        }
+        const bool staged = sd.npiece <= (uint32_t)SPAN_PIECES;
+        const Piece* list = staged ? sp_pieces : pieces + sd.piece0;
+        const int nlist = (int)sd.npiece;
+        __syncthreads();  // the previous span's threads are done with sp_pieces and next_span
+        if (staged)
+            for (int i = threadIdx.x; i < nlist; i += blockDim.x) sp_pieces[i] = pieces[sd.piece0 + i];
+        if (threadIdx.x == 0) next_span = atomicAdd(work, 1u) + gridDim.x;
+        int j = -1;  // this thread's current piece (its positions only move forward)
+        uint64_t end = 0, delta = 0;
         for (uint64_t tb = s0; tb < s1; tb += TILE) {
             const int n = (int)(s1 - tb < (uint64_t)TILE ? s1 - tb : (uint64_t)TILE);
-            __syncthreads();
-            if (threadIdx.x == 0) {  // the pieces overlapping [tb, tb + n)
-                int pc = pcur;
-                while (tb >= pieces[pc].dst + pieces[pc].len) pc++;
-                pcur = pc;
-                int m = 0;
-                while (m < TILE_PIECES && pc + m < npieces && pieces[pc + m].dst < tb + n) {
-                    tp[m] = pieces[pc + m];
-                    m++;
-                }
-                ntp = (pc + m < npieces && pieces[pc + m].dst < tb + n) ? 0 : m;  // 0: too many, search globally
-            }
-            __syncthreads();
-            const int m = ntp;
-            const int i0 = threadIdx.x * TPT;
-            uint32_t v[TPT];
-            int j = -1;
-            Piece pc{};
+            const uint32_t t0 = (uint32_t)(tb - s0);
+            __syncthreads();  // pieces staged; the previous tile's stores visible, its shared values read
 #pragma unroll
             for (int k = 0; k < TPT; k++) {
-                v[k] = 0;
-                if (i0 + k < n) {
-                    uint64_t p = tb + i0 + k;
-                    if (j < 0 || p >= pc.dst + pc.len) {
-                        j = piece_of(tp, m, pieces, npieces, p);
-                        pc = m > 0 ? tp[j] : pieces[j];
-                    }
-                    v[k] = pool[pc.src + (p - pc.dst)];
+                const int i = k * R1_THREADS + (int)threadIdx.x;
+                if (i >= n) continue;
+                const uint64_t p = tb + i;
+                if (j < 0) {
+                    j = piece_at(list, nlist, p);
+                    end = list[j].dst + list[j].len;
+                    delta = list[j].src - list[j].dst;  // pool index = position + delta
                 }
-            }
-            uint16_t r[TPT], q[TPT];
-            int64_t g[TPT];
-#pragma unroll
-            for (int k = 0; k < TPT; k++) {
-                const int i = i0 + k;
-                uint64_t p = tb + i;
-                r[k] = (uint16_t)v[k];
-                q[k] = (uint16_t)i;
-                g[k] = -1;
-                if (i < n && v[k] > REF) {
-                    int64_t src = (int64_t)p - (int64_t)(v[k] - REF);
-                    if (src < (int64_t)s0) {
-                        if (src < (int64_t)s0 - (int64_t)W) {
+                while (p >= end) {  // the next piece starts where this one ends
+                    j++;
+                    end = list[j].dst + list[j].len;
+                    delta = list[j].src - list[j].dst;
+                }
+                const uint32_t v = pool[p + delta];
+                uint32_t r = v, q = (uint32_t)i;
+                if (v > REF) {
+                    const int32_t src = (int32_t)(t0 + (uint32_t)i) - (int32_t)(v - REF);  // relative to s0
+                    if (src < 0) {
+                        if (src < -(int32_t)sd.W) {
                             bad[sd.stream] = 1;  // a match before the stream's start
-                            r[k] = 0;
+                            r = 0;
                         } else {
-                            r[k] = (uint16_t)(256 + (src - ((int64_t)s0 - (int64_t)WINDOW)));
+                            r = (uint32_t)(256 + (int32_t)WINDOW + src);  // byte of the entry window
                         }
-                    } else if ((uint64_t)src < tb) {
-                        g[k] = src;
+                    } else if ((uint32_t)src < t0) {
+                        r = out16[s0 + (uint32_t)src];  // resolved in an earlier tile
                     } else {
-                        r[k] = PENDING;
-                        q[k] = (uint16_t)((uint64_t)src - tb);
+                        r = PENDING;
+                        q = (uint32_t)src - t0;
                     }
                 }
-            }
-#pragma unroll
-            for (int k = 0; k < TPT; k++)
-                if (g[k] >= 0) r[k] = out16[g[k]];
-#pragma unroll
-            for (int k = 0; k < TPT; k++) {
-                if (i0 + k < n) {
-                    val[i0 + k] = r[k];
-                    ptr[i0 + k] = q[k];
-                }
+                val[i] = (uint16_t)r;
+                ptr[i] = (uint16_t)q;
             }
             __syncthreads();
             // copies inside the tile: pointer doubling until every chain reached a value
@@ -185,31 +154,28 @@ __global__ void __launch_bounds__(R1_THREADS) k_local(const uint16_t* __restrict
                 int pend = 0;
 #pragma unroll
                 for (int k = 0; k < TPT; k++) {
-                    int i = i0 + k;
+                    const int i = k * R1_THREADS + (int)threadIdx.x;
                     if (i < n && val[i] == PENDING) {
-                        uint16_t qq = ptr[i];
-                        uint16_t vq = val[qq];
+                        const uint16_t qq = ptr[i];
+                        const uint16_t vq = ((volatile uint16_t*)val)[qq];
                         if (vq != PENDING) {
                             val[i] = vq;
                         } else {
-                            ptr[i] = ptr[qq];
+                            ptr[i] = ((volatile uint16_t*)ptr)[qq];
                             pend = 1;
                         }
                     }
                 }
                 if (!__syncthreads_or(pend)) break;
             }
-            if (i0 + TPT <= n) {
-                uint2 w2;
-                w2.x = (uint32_t)val[i0] | (uint32_t)val[i0 + 1] << 16;
-                w2.y = (uint32_t)val[i0 + 2] | (uint32_t)val[i0 + 3] << 16;
-                *(uint2*)(out16 + tb + i0) = w2;
-            } else {
-                for (int k = 0; k < TPT; k++)
-                    if (i0 + k < n) out16[tb + i0 + k] = val[i0 + k];
+#pragma unroll
+            for (int k = 0; k < TPT; k++) {
+                const int i = k * R1_THREADS + (int)threadIdx.x;
+                if (i < n) out16[tb + i] = val[i];
             }
         }
         __syncthreads();
+        sp = next_span;
     }
 }
 
@@ -653,6 +619,17 @@ __global__ void k_crc_streams(const SpanDesc* __restrict__ spans, const uint32_t
 
 // ---------------------------------------------------------------- host side
 
+void span_pieces(SpanDesc* spans, uint64_t nspans, const Piece* pieces, uint64_t npieces) {
+    uint64_t p = 0;
+    for (uint64_t k = 0; k < nspans; k++) {
+        while (p < npieces && pieces[p].dst + pieces[p].len <= spans[k].start) p++;
+        uint64_t q = p;
+        while (q < npieces && pieces[q].dst < spans[k].end) q++;
+        spans[k].piece0 = (uint32_t)p;
+        spans[k].npiece = (uint32_t)(q - p);
+    }
+}
+
 static uint32_t mulmod_host(uint32_t a, uint32_t b) {
     uint32_t p = 0;
     for (int i = 0; i < 32; i++) {
@@ -728,9 +705,20 @@ int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, i
     return 1;
 }
 
+// k_local's grid: as many blocks as fit on the GPU at once (they take spans from a queue)
+static unsigned local_grid(uint64_t nspans) {
+    int dev = 0, nsm = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local, R1_THREADS, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    uint64_t g = (uint64_t)nsm * (uint64_t)per_sm;
+    return (unsigned)(nspans < g ? nspans : g);
+}
+
 int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans, uint64_t nspans,
                    uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad,
-                   uint8_t* out, int passes, void* stream) {
+                   uint8_t* out, int passes, unsigned* work, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (!total || npieces <= 0) return 0;
     int launches = 0;
@@ -738,8 +726,8 @@ int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (passes & 1) {
-        uint64_t grid = nspans < (uint64_t)nsm * 4 ? nspans : (uint64_t)nsm * 4;
-        k_local<<<(unsigned)grid, R1_THREADS, 0, st>>>(pool, pieces, npieces, spans, nspans, out16, bad);
+        cudaMemsetAsync(work, 0, sizeof(unsigned), st);
+        k_local<<<local_grid(nspans), R1_THREADS, 0, st>>>(pool, pieces, npieces, spans, nspans, out16, bad, work);
         launches++;
     }
     if (passes & 2) {
@@ -764,7 +752,7 @@ int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const
 
 int launch_resolve_streams(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans,
                            uint64_t nspans, const StreamWindows& sw, uint16_t* out16, uint8_t* windows, int* bad,
-                           uint8_t* out, int passes, void* stream) {
+                           uint8_t* out, int passes, unsigned* work, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (!nspans || npieces <= 0) return 0;
     int launches = 0;
@@ -772,8 +760,8 @@ int launch_resolve_streams(const uint16_t* pool, const Piece* pieces, int npiece
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (passes & 1) {
-        uint64_t grid = nspans < (uint64_t)nsm * 4 ? nspans : (uint64_t)nsm * 4;
-        k_local<<<(unsigned)grid, R1_THREADS, 0, st>>>(pool, pieces, npieces, spans, nspans, out16, bad);
+        cudaMemsetAsync(work, 0, sizeof(unsigned), st);
+        k_local<<<local_grid(nspans), R1_THREADS, 0, st>>>(pool, pieces, npieces, spans, nspans, out16, bad, work);
         launches++;
     }
     if (passes & 2) {
