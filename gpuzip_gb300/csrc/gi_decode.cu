@@ -331,35 +331,35 @@ __device__ void fixed_tables(Tables& T, int lane) {
 // the output side of a decoder: 32-symbol groups staged across the lanes
 struct Out {
     uint16_t* base;   // current extent
-    uint64_t op;      // symbols in the current extent
-    uint64_t cap;
+    uint32_t op;      // symbols in the current extent (an extent holds at most 16 Mi + 65,793)
+    uint32_t cap;
     uint64_t done;    // symbols in earlier extents
     int ext;          // current extent index
     uint16_t stage;   // this lane's symbol of the current group
 };
 
 __device__ __forceinline__ void flush_partial(Out& o, int lane) {
-    uint32_t r = (uint32_t)(o.op & 31);
-    if (r && (uint32_t)lane < r) o.base[(o.op & ~31ull) + lane] = o.stage;
+    uint32_t r = o.op & 31;
+    if (r && (uint32_t)lane < r) o.base[(o.op & ~31u) + lane] = o.stage;
 }
 
 __device__ __forceinline__ void emit_lit(Out& o, uint32_t v, int lane) {
-    uint32_t r = (uint32_t)(o.op & 31);
+    uint32_t r = o.op & 31;
     if ((uint32_t)lane == r) o.stage = (uint16_t)v;
     o.op++;
     if (r == 31) o.base[o.op - 32 + lane] = o.stage;
 }
 
 __device__ __forceinline__ void emit_run(Out& o, uint32_t len, uint16_t v, int lane) {
-    uint32_t r = (uint32_t)(o.op & 31);
+    uint32_t r = o.op & 31;
     if ((uint32_t)lane - r < len) o.stage = v;
     if (r + len < 32) {
         o.op += len;
         return;
     }
-    uint64_t g = o.op & ~31ull;
+    uint32_t g = o.op & ~31u;
     o.base[g + lane] = o.stage;
-    uint64_t p = g + 32;
+    uint32_t p = g + 32;
     uint32_t rem = r + len - 32;
     // 16-byte stores: 256 symbols per instruction (p is a multiple of 32: 64-byte aligned)
     uint32_t w = (uint32_t)v | ((uint32_t)v << 16);
@@ -404,7 +404,7 @@ __device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, in
     }
     o.done += o.op;
     o.op = 0;
-    o.cap = want;
+    o.cap = (uint32_t)want;
     o.base = C.a.pool + off;
     o.ext = e;
     return true;
@@ -412,8 +412,8 @@ __device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, in
 
 // Decodes one symbol of the current block and writes its output: 0 a literal or a match, 1 the
 // end-of-block code, -1 invalid data (no code, a length or distance symbol that does not exist,
-// or - check_refs - a match reaching before the stream's start). used: the bits it took.
-__device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int lane, bool check_refs, uint32_t& used) {
+// or - check_refs - a match reaching before the stream's start).
+__device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int lane, bool check_refs) {
     br.need(32);
     uint32_t e = T.lit[(uint32_t)br.buf & ((1u << LB) - 1)];
     if (e < (1u << 24)) {  // literal
@@ -421,7 +421,6 @@ __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int
         br.buf >>= n;
         br.cnt -= n;
         emit_lit(o, (e >> 8) & 255, lane);
-        used = (uint32_t)n;
         return 0;
     }
     if ((e & 15) == 0) {
@@ -432,7 +431,6 @@ __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int
             br.buf >>= n;
             br.cnt -= n;
             emit_lit(o, (e >> 8) & 255, lane);
-            used = (uint32_t)n;
             return 0;
         }
     }
@@ -441,7 +439,6 @@ __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int
         int n = (int)(e & 15);
         br.buf >>= n;
         br.cnt -= n;
-        used = (uint32_t)n;
         return 1;
     }
     if (kind == K_BAD) return -1;
@@ -462,7 +459,6 @@ __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int
     br.cnt -= dn + dx;
     if (check_refs && d > o.done + o.op) return -1;
     emit_run(o, len, (uint16_t)(REF + d), lane);
-    used = (uint32_t)(n + x + dn + dx);
     return 0;
 }
 
@@ -674,19 +670,18 @@ __device__ void decode_job(Ctx& C, int k) {
                     break;
                 }
             }
-            // a run of symbols with no per-symbol position or room checks: while at least 48 bits
-            // (the longest symbol) remain before the next check point and 258 symbols (the longest
-            // match) of room, no symbol can reach a target, the stop bit or the extent's end
-            int64_t left = (int64_t)(lim2 - p) - 48;
-            int64_t room = (int64_t)(o.cap - o.op) - (int64_t)MAX_SYMBOL_OUT;
+            // a run of symbols with no per-symbol position or room checks: a symbol takes at most
+            // 48 bits and writes at most 258 positions, so these cannot pass the next check point
+            // (the first one starts before it), the stop bit or the extent's end
+            const uint64_t left = lim2 - p;
+            const uint32_t room = o.cap - o.op;
+            uint32_t run = (uint32_t)(left / 48 < (uint64_t)(room / MAX_SYMBOL_OUT) ? left / 48 : room / MAX_SYMBOL_OUT);
+            if (run == 0) run = 1;
+            const bool chk = check_refs && r.blocks <= FIRST_RUN_BLOCKS;
             int rc;
             do {
-                uint32_t used;
-                const uint64_t op0 = o.op;
-                rc = one_symbol(T, br, o, lane, check_refs && r.blocks <= FIRST_RUN_BLOCKS, used);
-                left -= used;
-                room -= (int64_t)(o.op - op0);
-            } while (rc == 0 && left > 0 && room > 0);
+                rc = one_symbol(T, br, o, lane, chk);
+            } while (rc == 0 && --run);
             if (rc > 0) {
                 eob = true;
                 break;
