@@ -156,6 +156,15 @@ int decode_blocks_per_sm();
 int launch_decode(const DecodeArgs& a, int grid, void* stream);
 int launch_probe(const ProbeArgs& a, int grid, void* stream);
 int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream);
+// byte ranges the GPU reads directly (page-locked host or device memory) copied into dst: one
+// kernel for all of them; each piece at most GATHER_PIECE bytes
+constexpr uint64_t GATHER_PIECE = 256 << 10;
+struct GatherPiece {
+    const uint8_t* src;
+    uint64_t dst;  // offset in dst
+    uint64_t len;
+};
+int launch_gather(const GatherPiece* pieces, uint64_t n, uint8_t* dst, void* stream);
 // the output is resolved in spans of at most this many positions (a multiple of 16, at least WINDOW)
 constexpr uint64_t SPAN = 512 * 1024;
 // a span of output positions [start, end) of one stream; W: bytes of that stream before start that

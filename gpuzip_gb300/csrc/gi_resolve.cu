@@ -699,6 +699,46 @@ int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scra
     return launches;
 }
 
+// ---------------------------------------------------------------- gather
+
+// a block per piece: 16-byte loads and stores where source and destination agree modulo 16,
+// 4-byte ones where they agree modulo 4, bytes otherwise (the destination offsets are 4 KiB-aligned)
+__global__ void k_gather(const GatherPiece* __restrict__ pieces, uint64_t n, uint8_t* __restrict__ dst) {
+    for (uint64_t b = blockIdx.x; b < n; b += gridDim.x) {
+        const GatherPiece pc = pieces[b];
+        const uint8_t* src = pc.src;
+        uint8_t* d = dst + pc.dst;
+        const uint64_t len = pc.len;
+        const uintptr_t mis = ((uintptr_t)src ^ (uintptr_t)d);
+        if ((mis & 15) == 0) {
+            const uint64_t head = ((16 - ((uintptr_t)d & 15)) & 15) < len ? ((16 - ((uintptr_t)d & 15)) & 15) : len;
+            if (threadIdx.x < head) d[threadIdx.x] = src[threadIdx.x];
+            const uint64_t body = (len - head) / 16;
+            const uint4* s4 = (const uint4*)(src + head);
+            uint4* d4 = (uint4*)(d + head);
+            for (uint64_t i = threadIdx.x; i < body; i += blockDim.x) d4[i] = s4[i];
+            for (uint64_t i = head + body * 16 + threadIdx.x; i < len; i += blockDim.x) d[i] = src[i];
+        } else if ((mis & 3) == 0) {
+            const uint64_t head = ((4 - ((uintptr_t)d & 3)) & 3) < len ? ((4 - ((uintptr_t)d & 3)) & 3) : len;
+            if (threadIdx.x < head) d[threadIdx.x] = src[threadIdx.x];
+            const uint64_t body = (len - head) / 4;
+            const uint32_t* s4 = (const uint32_t*)(src + head);
+            uint32_t* d4 = (uint32_t*)(d + head);
+            for (uint64_t i = threadIdx.x; i < body; i += blockDim.x) d4[i] = s4[i];
+            for (uint64_t i = head + body * 4 + threadIdx.x; i < len; i += blockDim.x) d[i] = src[i];
+        } else {
+            for (uint64_t i = threadIdx.x; i < len; i += blockDim.x) d[i] = src[i];
+        }
+    }
+}
+
+int launch_gather(const GatherPiece* pieces, uint64_t n, uint8_t* dst, void* stream) {
+    if (!n) return 0;
+    uint64_t grid = n < 152 * 8 ? n : 152 * 8;
+    k_gather<<<(unsigned)grid, 256, 0, (cudaStream_t)stream>>>(pieces, n, dst);
+    return 1;
+}
+
 int launch_stored(const uint8_t* d_in, uint16_t* pool, const StoredCopy* list, int n, void* stream) {
     if (n <= 0) return 0;
     k_stored<<<n < 65535 ? n : 65535, 256, 0, (cudaStream_t)stream>>>(d_in, pool, list, n);

@@ -41,6 +41,7 @@ EXPORTED = (
 
 GI_STREAM_GZIP = 1
 GI_STREAM_CRC = 2
+GI_STREAM_MAPPED = 4
 
 
 class Config(ctypes.Structure):

@@ -125,9 +125,12 @@ GI_API int gi_inflate_gzip(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, gi_
  * (src/extract.rs:458-597). */
 #define GI_STREAM_GZIP 1u /* `in` is a gzip member: header parsed, trailer CRC-32 and ISIZE checked */
 #define GI_STREAM_CRC 2u  /* expected_crc holds the output's CRC-32 (a ZIP entry): checked */
+#define GI_STREAM_MAPPED 4u /* `in` is memory the GPU reads directly (page-locked host memory from
+                             * cudaHostAlloc/cudaHostRegister, or device memory): such streams are
+                             * gathered by one kernel instead of one copy call each */
 
 typedef struct {
-    const uint8_t* in;     /* the stream (host memory) */
+    const uint8_t* in;     /* the stream (host memory; see GI_STREAM_MAPPED) */
     uint64_t in_size;
     uint32_t flags;        /* GI_STREAM_GZIP, GI_STREAM_CRC */
     uint32_t expected_crc;

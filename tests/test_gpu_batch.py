@@ -126,3 +126,43 @@ def test_batch_high_ratio_members_in_one_pass(gpu):
     for i, (r, want) in enumerate(zip(res, wants)):
         assert r["status"] == 0 and r["output"] == want, i
     assert st.segments == 1
+
+
+def test_batch_mapped_inputs_are_gathered(gpu):
+    # streams in page-locked host memory (GI_STREAM_MAPPED): read by the gather kernel, at offsets of
+    # every alignment, mixed with ordinary host streams
+    import ctypes
+
+    import torch
+
+    texts = [W.log_text(90 + i, n, exact=True) for i, n in enumerate((1, 777, 70_000, 300_001, 1_000_003))]
+    members = [W.gzip_wrap(W.raw_deflate(t, 6), zlib.crc32(t), len(t)) for t in texts]
+    pinned = torch.empty(sum(len(m) + 64 for m in members), dtype=torch.uint8).pin_memory()
+    view = pinned.numpy()
+    arr = (gpuinflate.Stream * (2 * len(members)))()
+    import numpy as np
+
+    pos, keep = 16, []  # the first at a 16-byte boundary, the others at odd offsets
+    for i, m in enumerate(members):
+        view[pos:pos + len(m)] = np.frombuffer(m, dtype=np.uint8)
+        arr[i].in_ = ctypes.c_void_p(pinned.data_ptr() + pos)
+        arr[i].in_size = len(m)
+        arr[i].flags = gpuinflate.GI_STREAM_GZIP | gpuinflate.GI_STREAM_MAPPED
+        pos += len(m) + 1 + i  # every alignment case
+        b = ctypes.create_string_buffer(m, len(m))
+        keep.append(b)
+        j = len(members) + i
+        arr[j].in_ = ctypes.cast(b, ctypes.c_void_p)
+        arr[j].in_size = len(m)
+        arr[j].flags = gpuinflate.GI_STREAM_GZIP
+    total = 2 * sum(len(t) for t in texts) + 16 * 64 + (1 << 20)
+    out = ctypes.create_string_buffer(total)
+    st = gpuinflate.Stats()
+    rc = gpu.lib.gi_inflate_batch(gpu.ctx, arr, len(arr), ctypes.cast(out, ctypes.c_void_p), total, ctypes.byref(st))
+    assert rc == 0
+    for k in range(len(arr)):
+        want = texts[k % len(texts)]
+        a = arr[k]
+        assert a.status == 0, k
+        assert ctypes.string_at(ctypes.addressof(out) + a.out_offset, a.out_size) == want, k
+        assert a.crc32 == zlib.crc32(want)
