@@ -128,6 +128,12 @@ __global__ void __launch_bounds__(R1_THREADS, 4) k_local(const uint16_t* __restr
                     delta = list[j].src - list[j].dst;
                 }
                 const uint32_t v = pool[p + delta];
+                // the next tile's symbols of this piece into L2 while this tile resolves (one
+                // request per warp and step: the warp's 32 positions share a 64-byte line)
+                if ((threadIdx.x & 31) == 0 && p + TILE < end) {
+                    const uint16_t* nxt = pool + p + TILE + delta;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt));
+                }
                 uint32_t r = v, q = (uint32_t)i;
                 if (v > REF) {
                     const int32_t src = (int32_t)(t0 + (uint32_t)i) - (int32_t)(v - REF);  // relative to s0
