@@ -394,8 +394,16 @@ def run_serve(args, ws, rank, local):
         for key in ("submitted", "completed", "failed", "passes", "alone", "overlapped", "in_bytes", "out_bytes"):
             st[key] -= st0[key]
         st["busy_s"] = round(st["busy_s"] - st0["busy_s"], 3)
+        # where the slowest thousandth of the requests spent their time
+        slow = sorted(range(n), key=lambda k: -lat[k])[:max(1, n // 1000)]
+        ms = lambda v: round(v * 1e3, 2)
+        tail = [{"out_mb": round(want_size[k] / 2**20, 1), "latency_ms": ms(lat[k]),
+                 "admit_ms": ms(res[k]["t_admit"] - t_arr[k]), "queue_ms": ms(res[k]["t_start"] - res[k]["t_admit"]),
+                 "pass_ms": ms(res[k]["t_done"] - res[k]["t_start"]), "pass_requests": res[k]["pass_requests"]}
+                for k in slow[:5]]
         return {"gbs": round(good_out / span / 1e9, 3), "seconds": round(span, 3), "latency_ms": lat_summary(lat),
-                "wrong": len(bad), "mean_requests_per_pass": round(statistics.mean(batch), 2), "server": st}
+                "wrong": len(bad), "mean_requests_per_pass": round(statistics.mean(batch), 2), "server": st,
+                "slowest": tail}
 
     def plain(saturate):
         g = gpuinflate.Gpu(local)
@@ -495,7 +503,7 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--pool", type=int, default=256, help="serve: distinct members requests draw from")
-    ap.add_argument("--workers", type=int, default=2, help="serve: concurrent decode loops")
+    ap.add_argument("--workers", type=int, default=3, help="serve: concurrent decode loops")
     ap.add_argument("--hbm-budget", type=float, default=120e9)
     args = ap.parse_args()
     ws, rank, local = dist_env()

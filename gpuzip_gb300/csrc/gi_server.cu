@@ -43,6 +43,9 @@ constexpr uint32_t MIN_PASS_MB = 64;
 constexpr double CTX_BYTES_PER_PASS_BYTE = 12.0;  // a context's device memory per output byte of a pass
 constexpr uint64_t PASS_GAP = 1024 + 4096 + 8192;  // what a stream adds to a pass's input besides its bytes
 constexpr uint32_t MAX_WORKERS = 16;
+// a pass holds requests of one size class: large requests (a decode of tens of milliseconds) in
+// passes of their own, so small ones never wait for them inside a pass
+constexpr uint64_t LARGE_OUT = 32ull << 20;
 constexpr uint32_t MAX_BATCH = 65536;
 
 struct Request {
@@ -248,14 +251,20 @@ void work_loop(gi_server* s, int w) {
             b.push_back(f);
             s->ready.pop_front();
         } else {
+            // the ready requests of the first one's size class, in order, while they fit the pass
+            const bool large = f->out_guess >= LARGE_OUT;
             uint64_t in_b = 0, out_b = 0;
-            while (!s->ready.empty() && b.size() < s->cfg.max_batch) {
-                Request* r = s->ready.front();
+            for (auto it = s->ready.begin(); it != s->ready.end() && b.size() < s->cfg.max_batch;) {
+                Request* r = *it;
                 if (r->alone || r->pre_status != GI_OK) break;
+                if ((r->out_guess >= LARGE_OUT) != large) {
+                    ++it;
+                    continue;
+                }
                 if (!b.empty() && (in_b + r->size + PASS_GAP > s->pass_in || out_b + r->out_guess + 16 > s->pass_out))
                     break;
                 b.push_back(r);
-                s->ready.pop_front();
+                it = s->ready.erase(it);
                 in_b += r->size + PASS_GAP;
                 out_b += r->out_guess + 16;
             }
@@ -312,7 +321,7 @@ GI_API int gi_server_create(const gi_server_config* cfg, gi_done done, void* use
         if (cfg->size < sizeof(gi_server_config)) return fail(GI_ERR_ARG, "gi_server_config too small");
         c = *cfg;
     }
-    if (!c.workers) c.workers = 2;
+    if (!c.workers) c.workers = 3;
     if (c.workers > MAX_WORKERS) return fail(GI_ERR_ARG, "too many workers (at most 16)");
     if (!c.max_batch) c.max_batch = 4096;
     c.max_batch = std::min(c.max_batch, MAX_BATCH);

@@ -190,7 +190,7 @@ typedef struct gi_server gi_server;
 typedef struct {
     uint32_t size;          /* sizeof(gi_server_config) (40) */
     int32_t device;
-    uint32_t workers;       /* decode loops, i.e. passes that may run at once (0 = 2) */
+    uint32_t workers;       /* decode loops, i.e. passes that may run at once (0 = 3) */
     uint32_t max_batch;     /* most requests in one pass (0 = 4096) */
     uint32_t pass_out_mb;   /* output of one pass, MiB (0 = 2048, less when the budget is small) */
     uint32_t reserved;
