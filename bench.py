@@ -477,6 +477,89 @@ def run_serve(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_bgzf(args, ws, rank, local):
+    """A BGZF file (bgzip's 64 KiB members) of log text: every member in one gi_inflate_members
+    call (members decoded together) against one gi_inflate_gzip call per member (how gpuzip's host
+    decodes a gzip file, member by member)."""
+    import torch
+
+    from gpuzip_gb300 import gpuinflate
+    from gpuzip_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    os.makedirs(CACHE, exist_ok=True)
+    path = os.path.join(CACHE, f"bgzf_s1_{args.bgzf_mb}.gz")
+    if not os.path.exists(path):
+        data = W.log_text(1, args.bgzf_mb << 20, exact=True)
+        with open(path + ".tmp", "wb") as f:
+            f.write(W.bgzf(data))
+        os.replace(path + ".tmp", path)
+    with open(path, "rb") as f:
+        blob = f.read()
+    out_size = args.bgzf_mb << 20
+    pinned = torch.empty(len(blob), dtype=torch.uint8).pin_memory()
+    pinned.numpy()[:] = torch.frombuffer(bytearray(blob), dtype=torch.uint8).numpy()
+    ptr = ctypes.cast(pinned.data_ptr(), ctypes.c_char_p)
+    g = gpuinflate.Gpu(local)
+    lib = g.lib
+    info = gpuinflate.MembersInfo()
+    info.size = ctypes.sizeof(gpuinflate.MembersInfo)
+    stats = gpuinflate.Stats()
+
+    def batched():
+        rc = lib.gi_inflate_members(g.ctx, ptr, len(blob), gpuinflate.SINK(), None, ctypes.byref(info), ctypes.byref(stats))
+        if rc != 0 or stats.out_size != out_size:
+            raise RuntimeError(f"member decode failed: {rc} {lib.gi_last_error(g.ctx)}")
+
+    # member boundaries from the BGZF headers, for the one-call-per-member form
+    starts, pos = [], 0
+    while pos < len(blob):
+        starts.append(pos)
+        pos += int.from_bytes(blob[pos + 16:pos + 18], "little") + 1
+    msize = ctypes.c_uint64(0)
+
+    ends = starts[1:] + [len(blob)]
+
+    def plain():  # each call given exactly its member (gpuzip's host passes the rest of the file)
+        total = 0
+        for a, e in zip(starts, ends):
+            rc = lib.gi_inflate_gzip(g.ctx, ctypes.cast(pinned.data_ptr() + a, ctypes.c_char_p), e - a,
+                                     gpuinflate.SINK(), None, ctypes.byref(msize), ctypes.byref(stats))
+            if rc != 0:
+                raise RuntimeError(f"member at {a} failed: {rc}")
+            total += stats.out_size
+        if total != out_size:
+            raise RuntimeError("plain decode: wrong size")
+
+    for _ in range(args.warmup):
+        batched()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batched()
+    tb = (time.perf_counter() - t0) / args.steps
+    members = info.members
+    batched_members = info.batched
+    plain()
+    t0 = time.perf_counter()
+    plain()
+    tp = time.perf_counter() - t0
+    line = {
+        "metric": f"decompressed GB/s, a BGZF file of {members} members (64 KiB of log text each), whole-file call",
+        "value": round(out_size / tb / 1e9, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(tb * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"{args.bgzf_mb} MiB of log text (seed 1) as bgzip writes it: members of 65,280 input "
+                               f"bytes at level 6, {len(blob)} bytes compressed",
+                   "io": "pinned host memory in, output to the library's pinned buffers (no sink)"},
+        "members": members, "members_batched": batched_members,
+        "plain": {"value": round(out_size / tp / 1e9, 3), "unit": "GB/s", "calls": len(starts),
+                  "ms_per_call": round(tp / len(starts) * 1e3, 3)},
+        "whole_file_over_plain": round(tp / tb, 1),
+    }
+    print(json.dumps(line), flush=True)
+    g.close()
+
+
 def config_of(args, info):
     return {"workload": f"one gzip member, {args.nseg} x 1 MiB segments of mixed content (seed {args.seed}), levels 1/6/9 "
                         "in one Deflate stream",
@@ -497,7 +580,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="one device-resident decode, no timing (for ncu)")
-    ap.add_argument("--workload", default="member", choices=["member", "batch", "serve"])
+    ap.add_argument("--workload", default="member", choices=["member", "batch", "serve", "bgzf"])
     ap.add_argument("--nstreams", type=int, default=10000)
     ap.add_argument("--batch-total", type=float, default=8e9)
     ap.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
@@ -505,10 +588,14 @@ def main():
     ap.add_argument("--pool", type=int, default=256, help="serve: distinct members requests draw from")
     ap.add_argument("--workers", type=int, default=3, help="serve: concurrent decode loops")
     ap.add_argument("--hbm-budget", type=float, default=120e9)
+    ap.add_argument("--bgzf-mb", type=int, default=256, help="bgzf: MiB of output")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.workload == "serve":
         run_serve(args, ws, rank, local)
+        return
+    if args.workload == "bgzf":
+        run_bgzf(args, ws, rank, local)
         return
     if args.workload == "batch":
         run_batch(args, ws, rank, local)

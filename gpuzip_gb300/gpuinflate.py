@@ -31,6 +31,7 @@ EXPORTED = (
     "gi_last_profile",
     "gi_crc32_device_noalloc",
     "gi_inflate_batch",
+    "gi_inflate_members",
     "gi_server_create",
     "gi_server_submit",
     "gi_server_drain",
@@ -87,6 +88,16 @@ class Stream(ctypes.Structure):
 
 
 SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t)
+
+
+class MembersInfo(ctypes.Structure):
+    """gi_members_info (gpuinflate.h)"""
+
+    _fields_ = [("size", ctypes.c_uint32), ("members", ctypes.c_uint32), ("batched", ctypes.c_uint64),
+                ("trailing", ctypes.c_uint64), ("trailing_zero", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("size", "reserved")}
 
 
 class ServerConfig(ctypes.Structure):
@@ -172,6 +183,9 @@ def load(path=None):
     lib.gi_crc32_device_noalloc.restype = ctypes.c_int
     lib.gi_inflate_batch.argtypes = [vp, ctypes.POINTER(Stream), ctypes.c_uint32, vp, u64, ctypes.POINTER(Stats)]
     lib.gi_inflate_batch.restype = ctypes.c_int
+    lib.gi_inflate_members.argtypes = [vp, ctypes.c_char_p, u64, SINK, vp, ctypes.POINTER(MembersInfo),
+                                       ctypes.POINTER(Stats)]
+    lib.gi_inflate_members.restype = ctypes.c_int
     lib.gi_server_create.argtypes = [ctypes.POINTER(ServerConfig), DONE, vp, ctypes.POINTER(vp), ctypes.c_char_p,
                                      ctypes.c_size_t]
     lib.gi_server_create.restype = ctypes.c_int
@@ -273,6 +287,32 @@ class Gpu:
             if rc != GI_OK:
                 raise self._error(rc)
         return b"".join(parts), msize.value, st
+
+    def inflate_members(self, data, sink=None):
+        """Every gzip member of `data` (gi_inflate_members). Returns (output bytes or None when a
+        sink is given, info dict, Stats); raises InflateError on a failure."""
+        parts = []
+
+        def _cb(user, ptr, n):
+            try:
+                chunk = ctypes.string_at(ptr, n)
+                if sink is not None:
+                    return 0 if sink(chunk) else 1
+                parts.append(chunk)
+                return 0
+            except Exception:
+                return 1
+
+        info = MembersInfo()
+        info.size = ctypes.sizeof(MembersInfo)
+        st = Stats()
+        buf = bytes(data)
+        with self._lock:
+            rc = self.lib.gi_inflate_members(self.ctx, buf, len(buf), SINK(_cb), None, ctypes.byref(info),
+                                             ctypes.byref(st))
+            if rc != GI_OK:
+                raise self._error(rc)
+        return (b"".join(parts) if sink is None else None), info.as_dict(), st
 
     def inflate_device(self, d_in, in_size, d_out, out_cap):
         """Device-resident form: pointers (ints) to GPU memory. Returns (out_size, Stats)."""

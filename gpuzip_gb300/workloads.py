@@ -397,3 +397,24 @@ def zero_sector(member, seed, index):
     a, e = max(lo, sec * 4096), min(hi, sec * 4096 + 4096)
     b[a:e] = bytes(e - a)
     return bytes(b)
+
+
+def bgzf(data, block=0xFF00, level=6):
+    """`data` as a BGZF file (bgzip's format): gzip members of at most `block` input bytes, each
+    header carrying the "BC" extra subfield with the member's size less one, then the empty
+    end-of-file member."""
+    out = bytearray()
+    for a in range(0, len(data) + 1, block):
+        chunk = data[a:a + block]
+        if not chunk and a:
+            break
+        body = raw_deflate(chunk, level)
+        bsize = 12 + 6 + len(body) + 8  # header with XLEN, the subfield, body, trailer
+        out += bytes([0x1F, 0x8B, 8, 4, 0, 0, 0, 0, 0, 0xFF, 6, 0, ord("B"), ord("C"), 2, 0])
+        out += (bsize - 1).to_bytes(2, "little") + body
+        out += zlib.crc32(chunk).to_bytes(4, "little") + len(chunk).to_bytes(4, "little")
+    # the end-of-file marker: an empty member
+    empty = raw_deflate(b"", level)
+    out += bytes([0x1F, 0x8B, 8, 4, 0, 0, 0, 0, 0, 0xFF, 6, 0, ord("B"), ord("C"), 2, 0])
+    out += (12 + 6 + len(empty) + 8 - 1).to_bytes(2, "little") + empty + bytes(8)
+    return bytes(out)

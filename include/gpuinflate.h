@@ -172,6 +172,29 @@ GI_API int gi_last_profile(const gi_ctx* ctx, gi_profile* profile);
 GI_API int gi_crc32_device_noalloc(int device, const void* d_data, uint64_t size, uint32_t* d_crc, void* stream,
                                    char* err, size_t err_len);
 
+/* Every gzip member of a file (a .gz, .tgz, a BGZF file, any concatenation of members), decoded
+ * as gpuzip's gz::decode does (src/gz.rs:154-264): header rules of parse_header (FHCRC checked,
+ * BGZF's "BC" subfield read), each member's trailer CRC-32 and ISIZE checked against values
+ * computed on the GPU, the outputs handed to `sink` in order, from a thread the library owns,
+ * never two calls at once. After the first member, bytes that are not a gzip member end the
+ * file: they are ignored and reported in *info. Members whose size their BGZF header gives are
+ * decoded together, many per pass of the batched form (no per-member call); the others one by
+ * one through the segmented path. Errors: GI_ERR_DATA (not gzip, no member, a bad header, invalid
+ * Deflate data, a CRC or size mismatch), GI_ERR_TRUNCATED (the input ends inside a member),
+ * GI_ERR_ABORTED (the sink stopped), GI_ERR_GPU. No counterpart in the reference, whose host
+ * decodes member by member (about 10 ms of GPU call each, src/gz.rs:16-19). */
+typedef struct {
+    uint32_t size;          /* sizeof(gi_members_info), set by the caller (32) */
+    uint32_t members;       /* members decoded */
+    uint64_t batched;       /* of which decoded together (their size from a BGZF header) */
+    uint64_t trailing;      /* bytes after the last member that are not a gzip member */
+    uint32_t trailing_zero; /* 1: those bytes are all zero */
+    uint32_t reserved;
+} gi_members_info;
+
+GI_API int gi_inflate_members(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, gi_sink sink, void* user,
+                              gi_members_info* info, gi_stats* stats);
+
 /* ------------------------------------------------------------------ part 3: the request server
  *
  * A request loop over the batched form, for a process that decodes many streams as they come

@@ -90,3 +90,7 @@ def test_server_bad_arguments_without_gpu(lib):
     assert lib.gi_server_read_stats(None, ctypes.byref(st)) == gpuinflate.GI_ERR_ARG
     assert lib.gi_server_clock(None) == 0.0
     lib.gi_server_destroy(None)
+
+
+def test_members_info_layout():
+    assert ctypes.sizeof(gpuinflate.MembersInfo) == 32
