@@ -32,6 +32,7 @@ EXPORTED = (
     "gi_crc32_device_noalloc",
     "gi_inflate_batch",
     "gi_inflate_members",
+    "gi_inflate_zip",
     "gi_server_create",
     "gi_server_submit",
     "gi_server_drain",
@@ -98,6 +99,18 @@ class MembersInfo(ctypes.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k not in ("size", "reserved")}
+
+
+class ZipEntry(ctypes.Structure):
+    """gi_zip_entry (gpuinflate.h)"""
+
+    _fields_ = [("size", ctypes.c_uint32), ("index", ctypes.c_uint32), ("method", ctypes.c_uint16),
+                ("flags", ctypes.c_uint16), ("status", ctypes.c_int32), ("out_size", ctypes.c_uint64),
+                ("in_size", ctypes.c_uint64), ("crc32", ctypes.c_uint32), ("name_len", ctypes.c_uint32)]
+
+
+ENTRY_SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ZipEntry), ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_size_t)
 
 
 class ServerConfig(ctypes.Structure):
@@ -186,6 +199,8 @@ def load(path=None):
     lib.gi_inflate_members.argtypes = [vp, ctypes.c_char_p, u64, SINK, vp, ctypes.POINTER(MembersInfo),
                                        ctypes.POINTER(Stats)]
     lib.gi_inflate_members.restype = ctypes.c_int
+    lib.gi_inflate_zip.argtypes = [vp, ctypes.c_char_p, u64, ENTRY_SINK, vp, ctypes.POINTER(Stats)]
+    lib.gi_inflate_zip.restype = ctypes.c_int
     lib.gi_server_create.argtypes = [ctypes.POINTER(ServerConfig), DONE, vp, ctypes.POINTER(vp), ctypes.c_char_p,
                                      ctypes.c_size_t]
     lib.gi_server_create.restype = ctypes.c_int
@@ -313,6 +328,34 @@ class Gpu:
             if rc != GI_OK:
                 raise self._error(rc)
         return (b"".join(parts) if sink is None else None), info.as_dict(), st
+
+    def inflate_zip(self, data, stop_after=None):
+        """Every entry of the ZIP archive `data` (gi_inflate_zip). Returns (list of dicts in
+        directory order: index, name, method, flags, status, out_size, crc32, output (bytes, or
+        None when not decoded), Stats). stop_after: the sink stops after this many calls."""
+        entries = {}
+        calls = [0]
+
+        def _cb(user, ep, name, data_ptr, n):
+            e = ep.contents
+            d = entries.setdefault(e.index, {"index": e.index, "name": ctypes.string_at(name, e.name_len).decode("utf-8", "replace"),
+                                             "method": e.method, "flags": e.flags, "out_size": e.out_size,
+                                             "crc32": e.crc32, "output": None})
+            d["status"] = e.status
+            if data_ptr and n:
+                d["output"] = (d["output"] or b"") + ctypes.string_at(data_ptr, n)
+            elif e.status == GI_OK and d["output"] is None:
+                d["output"] = b""
+            calls[0] += 1
+            return 1 if stop_after is not None and calls[0] >= stop_after else 0
+
+        st = Stats()
+        buf = bytes(data)
+        with self._lock:
+            rc = self.lib.gi_inflate_zip(self.ctx, buf, len(buf), ENTRY_SINK(_cb), None, ctypes.byref(st))
+            if rc != GI_OK:
+                raise self._error(rc)
+        return [entries[k] for k in sorted(entries)], st
 
     def inflate_device(self, d_in, in_size, d_out, out_cap):
         """Device-resident form: pointers (ints) to GPU memory. Returns (out_size, Stats)."""

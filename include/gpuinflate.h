@@ -195,6 +195,39 @@ typedef struct {
 GI_API int gi_inflate_members(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, gi_sink sink, void* user,
                               gi_members_info* info, gi_stats* stats);
 
+/* Every entry of a ZIP archive, read as gpuzip's zip.rs reads it (read_central_directory and plan,
+ * src/zip.rs:393-540): the end record (Zip64 when present), data prepended to the archive, the
+ * central directory with its Zip64 extra fields, each entry's local header, entries whose bytes
+ * overlap another's (a zip bomb's trick) left out. Deflate entries are decoded together, many per
+ * pass of the batched form, each checked against the directory's CRC-32 and size; stored entries
+ * are checked the same way; directories, encrypted entries and other methods are not decoded.
+ * The sink gets every entry in directory order, from a thread the library owns, never two calls
+ * at once: once per entry (several times, consecutive, for an entry of more than 256 MiB, then
+ * once more with data NULL if it failed after its output began), with data NULL when the entry
+ * has no output (status says why). A nonzero return stops the call.
+ * Returns GI_OK when the directory could be read (entries may fail one by one), GI_ERR_DATA
+ * when it cannot ("not a ZIP file", a bad or truncated directory, a bad local header),
+ * GI_ERR_ABORTED, GI_ERR_GPU. No counterpart in the reference (its extract.rs sends each large
+ * entry to gi_inflate and batches small ones through nvCOMP, src/extract.rs:320-597). */
+typedef struct {
+    uint32_t size;     /* sizeof(gi_zip_entry) (40) */
+    uint32_t index;    /* position in the central directory */
+    uint16_t method;   /* 0 stored, 8 deflated, another number: not decoded */
+    uint16_t flags;    /* the entry's general-purpose flags (bit 0: encrypted) */
+    int32_t status;    /* GI_OK; GI_ERR_DATA (invalid data, or a CRC or size mismatch); GI_ERR_TRUNCATED;
+                          GI_ERR_ARG: not decoded (a directory, encrypted, another method, overlapping) */
+    uint64_t out_size; /* its size in the directory */
+    uint64_t in_size;  /* its compressed size in the directory */
+    uint32_t crc32;    /* the directory's CRC-32 */
+    uint32_t name_len; /* bytes of the name passed with it */
+} gi_zip_entry;
+
+typedef int (*gi_entry_sink)(void* user, const gi_zip_entry* entry, const uint8_t* name, const uint8_t* data,
+                             size_t len);
+
+GI_API int gi_inflate_zip(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, gi_entry_sink sink, void* user,
+                          gi_stats* stats);
+
 /* ------------------------------------------------------------------ part 3: the request server
  *
  * A request loop over the batched form, for a process that decodes many streams as they come

@@ -94,3 +94,8 @@ def test_server_bad_arguments_without_gpu(lib):
 
 def test_members_info_layout():
     assert ctypes.sizeof(gpuinflate.MembersInfo) == 32
+
+
+def test_zip_entry_layout():
+    assert ctypes.sizeof(gpuinflate.ZipEntry) == 40
+    assert gpuinflate.ZipEntry.out_size.offset == 16
