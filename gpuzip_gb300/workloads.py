@@ -418,3 +418,22 @@ def bgzf(data, block=0xFF00, level=6):
     out += bytes([0x1F, 0x8B, 8, 4, 0, 0, 0, 0, 0, 0xFF, 6, 0, ord("B"), ord("C"), 2, 0])
     out += (12 + 6 + len(empty) + 8 - 1).to_bytes(2, "little") + empty + bytes(8)
     return bytes(out)
+
+
+def zip_archive(entries):
+    """A ZIP archive (stored as written by a plain archiver: local headers, data, the central
+    directory, the end record) of already-compressed entries: (name bytes, raw Deflate body,
+    CRC-32, uncompressed size), method 8 each. Offsets and sizes must stay below 4 GiB."""
+    out = bytearray()
+    cd = bytearray()
+    for name, body, crc, size in entries:
+        off = len(out)
+        out += struct.pack("<IHHHHHIIIHH", 0x04034B50, 20, 0, 8, 0, 0x21, crc, len(body), size, len(name), 0)
+        out += name + body
+        cd += struct.pack("<IHHHHHHIIIHHHHHII", 0x02014B50, 20, 20, 0, 8, 0, 0x21, crc, len(body), size, len(name),
+                          0, 0, 0, 0, 0, off)
+        cd += name
+    cd_off = len(out)
+    out += cd
+    out += struct.pack("<IHHHHIIH", 0x06054B50, 0, 0, len(entries), len(entries), len(cd), cd_off, 0)
+    return bytes(out)

@@ -179,8 +179,9 @@ GI_API int gi_crc32_device_noalloc(int device, const void* d_data, uint64_t size
  * never two calls at once. After the first member, bytes that are not a gzip member end the
  * file: they are ignored and reported in *info. Members whose size their BGZF header gives are
  * decoded together, many per pass of the batched form (no per-member call); the others one by
- * one through the segmented path. Errors: GI_ERR_DATA (not gzip, no member, a bad header, invalid
- * Deflate data, a CRC or size mismatch), GI_ERR_TRUNCATED (the input ends inside a member),
+ * one through the segmented path; a file in page-locked memory is read by the gather kernel.
+ * Errors: GI_ERR_DATA (not gzip, no member, a bad header, invalid Deflate data, a CRC or size
+ * mismatch), GI_ERR_TRUNCATED (the input ends inside a member),
  * GI_ERR_ABORTED (the sink stopped), GI_ERR_GPU. No counterpart in the reference, whose host
  * decodes member by member (about 10 ms of GPU call each, src/gz.rs:16-19). */
 typedef struct {
@@ -202,7 +203,7 @@ GI_API int gi_inflate_members(gi_ctx* ctx, const uint8_t* in, uint64_t in_size, 
  * pass of the batched form, each checked against the directory's CRC-32 and size; stored entries
  * are checked the same way; directories, encrypted entries and other methods are not decoded.
  * The sink gets every entry in directory order, from a thread the library owns, never two calls
- * at once: once per entry (several times, consecutive, for an entry of more than 256 MiB, then
+ * at once: once per entry (several times, consecutive, for an entry larger than a pass, then
  * once more with data NULL if it failed after its output began), with data NULL when the entry
  * has no output (status says why). A nonzero return stops the call.
  * Returns GI_OK when the directory could be read (entries may fail one by one), GI_ERR_DATA
