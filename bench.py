@@ -603,6 +603,131 @@ def run_bgzf(args, ws, rank, local):
     g.close()
 
 
+def rescue_workload(nfiles):
+    """(damaged .tar.gz bytes, info) of the rescue workload, cached on local disk between runs."""
+    from gpuzip_gb300 import workloads as W
+
+    os.makedirs(CACHE, exist_ok=True)
+    path = os.path.join(CACHE, f"rescue_tar_s4_{nfiles}.gz")
+    meta = path + ".json"
+    if not (os.path.exists(path) and os.path.exists(meta)):
+        member, info = W.rescue_tar(seed=4, nfiles=nfiles)
+        damaged, done = W.rescue_damage(member, seed=4)
+        info = {"crc": info["crc"], "size": info["size"], "member_bytes": len(member), "damage": done,
+                "files": len(info["files"])}
+        with open(path + ".tmp", "wb") as f:
+            f.write(damaged)
+        os.replace(path + ".tmp", path)
+        with open(meta, "w") as f:
+            json.dump(info, f)
+    with open(path, "rb") as f:
+        data = f.read()
+    with open(meta) as f:
+        info = json.load(f)
+    return data, info
+
+
+def run_rescue(args, ws, rank, local):
+    """The damaged .tar.gz (2,000 files of mixed content, three zeroed sectors, a span written
+    twice, CR LF to LF in a 16 MiB region) through gr_rescue: `value` with no sink (output and
+    mask left in device memory), `e2e` with a sink that copies every output byte and mask byte to
+    host memory."""
+    import numpy as np
+    import torch
+
+    from gpuzip_gb300 import gpuinflate, gzrescue
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "gzrescue's rescue library is built from the reference's "
+                              "gpuinflate/rescue.cpp, which is not present on this host"}), flush=True)
+        return
+    torch.cuda.set_device(local)
+    os.environ["GPUZIP_RESCUE_DEVICE"] = str(local)
+    data, info = rescue_workload(args.rescue_files)
+    pinned = torch.empty(len(data), dtype=torch.uint8).pin_memory()
+    pinned.numpy()[:] = np.frombuffer(data, dtype=np.uint8)
+    ptr = ctypes.cast(pinned.data_ptr(), ctypes.c_char_p)
+    lib = gzrescue.bind(gpuinflate.LIB_PATH)
+    opt = gzrescue.Options(ctypes.sizeof(gzrescue.Options), 0, 1, 0, 0, 0, 0)
+    out_cap = info["size"] + (64 << 20)
+    h_out = torch.empty(out_cap, dtype=torch.uint8).pin_memory()
+    h_mask = torch.empty(out_cap, dtype=torch.uint8).pin_memory()
+    pos = [0]
+    base_out, base_mask = h_out.data_ptr(), h_mask.data_ptr()
+
+    def take(_user, d, m, n):
+        if pos[0] + n > out_cap:
+            return 1
+        ctypes.memmove(base_out + pos[0], d, n)
+        ctypes.memmove(base_mask + pos[0], m, n)
+        pos[0] += n
+        return 0
+
+    sink = gzrescue.SINK(take)
+
+    def call(with_sink):
+        pos[0] = 0
+        res = ctypes.c_void_p()
+        rc = lib.gr_rescue(ptr, len(data), ctypes.byref(opt), sink if with_sink else gzrescue.SINK(), None,
+                           ctypes.byref(res))
+        if rc != 0 or not res.value:
+            raise RuntimeError(f"gr_rescue failed: {rc}")
+        st = lib.gr_result_stats(res).contents
+        s = {f: getattr(st, f) for f in gzrescue.STAT_FIELDS}
+        lib.gr_free(res)
+        if with_sink and pos[0] != s["output_size"]:
+            raise RuntimeError("the sink did not receive the whole output")
+        return s
+
+    for _ in range(args.warmup):
+        first = call(False)
+    with Clocks() as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s = call(False)
+            if s != first:
+                raise RuntimeError("rescue results differ between runs")
+        t = (time.perf_counter() - t0) / args.steps
+    launches = int(lib.gr_last_launches())
+    call(True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        se = call(True)
+    te = (time.perf_counter() - t0) / args.steps
+    if se != first:
+        raise RuntimeError("rescue results differ with a sink")
+    mask = h_mask.numpy()[:se["output_size"]]
+    counts = np.bincount(mask, minlength=4).tolist()
+    if counts[1] != se["exact_bytes"] or counts[2] != se["suspect_bytes"] or counts[0] != se["unknown_bytes"]:
+        raise RuntimeError(f"mask counts {counts} disagree with the statistics {se}")
+    out = s["output_size"]
+    line = {
+        "metric": "rescued GB/s (output bytes), a damaged 2,000-file .tar.gz of mixed content, 1 GB300",
+        "value": round(out / t / 1e9, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(t * 1e3, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"a .tar.gz of {info['files']} files (sizes log-uniform over [4 KiB, 8 MiB], contents of the "
+                               "mixed workload, seed 4), the tar stream in 1 MiB segments at levels 1/6/9 in one Deflate stream; "
+                               f"{info['size']} bytes of tar, {len(data)} bytes damaged: three 4 KiB sectors zeroed, a 64 KiB "
+                               f"span written twice, CR LF to LF in a 16 MiB region ({info['damage']['crlf'][1]} CRs lost)",
+                   "options": "no_infer 1 (the inference of lost window bytes is not done on this path)",
+                   "io": "value: host input (page-locked), output and mask left in device memory (no sink); e2e: every "
+                         "output and mask byte delivered to a host sink"},
+        "e2e": {"value": round(out / te / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": len(data),
+                "d2h_bytes_per_step": 2 * out},
+        "gpu_launches": launches,
+        "cpu_baseline": None,
+        "cpu_baseline_unavailable": "the reference's rescue library is built from its rescue.cpp, which is not on this host",
+        "result": {k: s[k] for k in ("output_size", "exact_bytes", "suspect_bytes", "unknown_bytes", "headers", "pieces",
+                                     "damaged", "crc_check", "hidden_damage")},
+        "mask_counts": counts,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def config_of(args, info):
     return {"workload": f"one gzip member, {args.nseg} x 1 MiB segments of mixed content (seed {args.seed}), levels 1/6/9 "
                         "in one Deflate stream",
@@ -623,7 +748,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="one device-resident decode, no timing (for ncu)")
-    ap.add_argument("--workload", default="member", choices=["member", "batch", "serve", "bgzf"])
+    ap.add_argument("--workload", default="member", choices=["member", "batch", "serve", "bgzf", "rescue"])
+    ap.add_argument("--rescue-files", type=int, default=2000, help="rescue: files in the .tar.gz")
     ap.add_argument("--nstreams", type=int, default=10000)
     ap.add_argument("--batch-total", type=float, default=8e9)
     ap.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
@@ -639,6 +765,9 @@ def main():
         return
     if args.workload == "bgzf":
         run_bgzf(args, ws, rank, local)
+        return
+    if args.workload == "rescue":
+        run_rescue(args, ws, rank, local)
         return
     if args.workload == "batch":
         run_batch(args, ws, rank, local)

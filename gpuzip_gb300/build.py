@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libgpuinflate.so")
-SOURCES = ["gi_find.cu", "gi_decode.cu", "gi_resolve.cu", "gi_engine.cu", "gi_noalloc.cu", "gi_server.cu"]
+SOURCES = ["gi_find.cu", "gi_decode.cu", "gi_resolve.cu", "gi_engine.cu", "gi_noalloc.cu", "gi_server.cu", "gi_rescue.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -34,7 +34,7 @@ def build(verbose=False, ptxas_info=False):
     def one(src):
         obj = os.path.join(bdir, src.replace(".cu", ".o"))
         srcp = os.path.join(CSRC, src)
-        deps = [srcp, os.path.join(ROOT, "include", "gpuinflate.h")] + [
+        deps = [srcp, os.path.join(ROOT, "include", "gpuinflate.h"), os.path.join(ROOT, "include", "gzrescue_gb300.h")] + [
             os.path.join(CSRC, h) for h in ("gi_common.cuh", "gi_internal.h", "gi_arena.h", "gi_find_cl.h")]
         if not ptxas_info and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
             return obj, ""

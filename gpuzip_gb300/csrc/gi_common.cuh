@@ -64,6 +64,9 @@ struct JobResult {
     uint32_t blocks;     // block headers read
     uint64_t cycles;     // SM clock cycles the job took (diagnostics)
     uint64_t hdr0;       // header of the first block it decoded symbols of (diagnostics)
+    uint64_t symbols;    // literals and matches decoded (an encoder's blocks hold a regular number)
+    uint64_t last_block_bit;  // header of the last block it began (UINT64_MAX: none)
+    uint64_t last_block_out;  // symbols written before that header
 };
 
 // a run of a job's output in the pool; job k's first extent is extent k
@@ -150,6 +153,10 @@ struct StoredCand {
 constexpr int FIND_SLOTS_PER_CHUNK = 4;
 int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
                 uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, const uint8_t* skip, void* stream);
+// every position in (bit_lo, bit_hi) that passes the full dynamic-header check, appended to out
+// in no order (*n counts them all, including those past cap)
+int launch_find_all(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint64_t end_bit,
+                    uint64_t* out, unsigned* n, unsigned cap, void* stream);
 int launch_stored_scan(const uint8_t* d_in, uint64_t byte_lo, uint64_t byte_hi, uint64_t end_word, uint64_t end_byte,
                        StoredCand* out, unsigned* n, unsigned cap, void* stream);
 int decode_blocks_per_sm();

@@ -411,8 +411,10 @@ __device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, in
 }
 
 // Decodes one symbol of the current block and writes its output: 0 a literal or a match, 1 the
-// end-of-block code, -1 invalid data (no code, a length or distance symbol that does not exist,
-// or - check_refs - a match reaching before the stream's start).
+// end-of-block code, -1 invalid data with no code at all, -2 invalid data after a length symbol
+// was read (a length or distance symbol that does not exist, or - check_refs - a match reaching
+// before the stream's start). The reference counts a symbol at its length code, before the rest
+// is checked (inflate.cuh:449-457), so a -2 is one more symbol read.
 __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int lane, bool check_refs) {
     br.need(32);
     uint32_t e = T.lit[(uint32_t)br.buf & ((1u << LB) - 1)];
@@ -441,7 +443,7 @@ __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int
         br.cnt -= n;
         return 1;
     }
-    if (kind == K_BAD) return -1;
+    if (kind == K_BAD) return -2;
     int n = (int)(e & 15), x = (int)((e >> 4) & 15);
     uint32_t len = ((e >> 8) & 0xffff) + (uint32_t)((br.buf >> n) & ((1u << x) - 1));
     br.buf >>= n + x;
@@ -450,14 +452,14 @@ __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int
     uint32_t de = T.dist[(uint32_t)br.buf & ((1u << DB) - 1)];
     if ((de & 15) == 0) {
         de = de == E_LONG ? slow_decode(T.distc, T.dist_syms, A_DIST, br.buf, DB) : 0;
-        if (de == 0) return -1;
+        if (de == 0) return -2;
     }
-    if ((de & (3u << 24)) == K_BAD) return -1;
+    if ((de & (3u << 24)) == K_BAD) return -2;
     int dn = (int)(de & 15), dx = (int)((de >> 4) & 15);
     uint32_t d = ((de >> 8) & 0xffff) + (uint32_t)((br.buf >> dn) & ((1u << dx) - 1));
     br.buf >>= dn + dx;
     br.cnt -= dn + dx;
-    if (check_refs && d > o.done + o.op) return -1;
+    if (check_refs && d > o.done + o.op) return -2;
     emit_run(o, len, (uint16_t)(REF + d), lane);
     return 0;
 }
@@ -488,6 +490,9 @@ __device__ void decode_job(Ctx& C, int k) {
     r.blocks = 0;
     r.resume = J.start;
     r.hdr0 = UINT64_MAX;
+    r.symbols = 0;
+    r.last_block_bit = UINT64_MAX;
+    r.last_block_out = 0;
 
     Out o;
     o.base = C.a.pool + J.pool_off;
@@ -557,6 +562,8 @@ __device__ void decode_job(Ctx& C, int k) {
                 break;
             }
             header = p;
+            r.last_block_bit = p;
+            r.last_block_out = o.done + o.op;
             int fin = (int)br.get(1);
             int type = (int)br.get(2);
             r.blocks++;
@@ -679,15 +686,18 @@ __device__ void decode_job(Ctx& C, int k) {
             if (run == 0) run = 1;
             const bool chk = check_refs && r.blocks <= FIRST_RUN_BLOCKS;
             int rc;
+            const uint32_t run0 = run;
             do {
                 rc = one_symbol(T, br, o, lane, chk);
             } while (rc == 0 && --run);
+            r.symbols += run0 - run;  // every symbol but the one that ended the run early was a literal or match
             if (rc > 0) {
                 eob = true;
                 break;
             }
             if (rc < 0) {
                 r.status = S_DATA;
+                r.symbols += rc == -2;
                 break;
             }
         }

@@ -167,11 +167,16 @@ __device__ bool verify_header(const uint32_t* w, uint64_t end_word, uint64_t end
 constexpr int LIST = 1024 + 64;
 constexpr int FIND_SLOTS = 4;  // block starts kept per chunk (a short block can share a chunk with the next)
 
+// ALL: every verified candidate is appended to all_out (in no order; all_n counts them, past
+// all_cap too) instead of the chunk's first FIND_SLOTS going to `first`
+template <bool ALL>
 __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __restrict__ w, uint64_t bit_lo,
                                                           uint64_t bit_hi, uint64_t end_word, uint64_t end_bit,
                                                           uint32_t chunk_bits, uint64_t nchunks,
                                                           uint64_t* __restrict__ first,
-                                                          const uint8_t* __restrict__ skip) {
+                                                          const uint8_t* __restrict__ skip,
+                                                          uint64_t* __restrict__ all_out, unsigned* __restrict__ all_n,
+                                                          unsigned all_cap) {
     __shared__ uint32_t cand[FIND_WARPS][LIST];  // candidate bit, relative to the chunk's first word
     __shared__ uint16_t cl4[CL4_ENTRIES];         // Kraft contributions of four code-length fields
     for (int i = threadIdx.x; i < CL4_ENTRIES; i += blockDim.x) cl4[i] = cl4_entry((uint32_t)i);
@@ -199,6 +204,13 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
                         ok = verify_header(w, end_word, end_bit, bit);
                     }
                     uint32_t bal = __ballot_sync(FULL, ok);
+                    if (ALL) {
+                        if (ok) {
+                            unsigned q = atomicAdd(all_n, 1u);
+                            if (q < all_cap) all_out[q] = bit;
+                        }
+                        continue;
+                    }
                     while (bal && nfound < FIND_SLOTS) {
                         uint64_t b = __shfl_sync(FULL, bit, __ffs(bal) - 1);
                         if (lane == nfound) found = b;
@@ -265,7 +277,7 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
             }
             if (!done && nlist) drain(nlist);
         }
-        if (lane < FIND_SLOTS) first[c * FIND_SLOTS + lane] = found;
+        if (!ALL && lane < FIND_SLOTS) first[c * FIND_SLOTS + lane] = found;
     }
 }
 
@@ -311,8 +323,23 @@ int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t 
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     uint64_t blocks = (nchunks + FIND_WARPS - 1) / FIND_WARPS;
     uint64_t cap = (uint64_t)nsm * 8;
-    k_find<<<(unsigned)(blocks < cap ? blocks : cap), FIND_WARPS * 32, 0, (cudaStream_t)stream>>>(
-        (const uint32_t*)d_in, bit_lo, bit_hi, end_word, end_bit, chunk_bits, nchunks, d_first, skip);
+    k_find<false><<<(unsigned)(blocks < cap ? blocks : cap), FIND_WARPS * 32, 0, (cudaStream_t)stream>>>(
+        (const uint32_t*)d_in, bit_lo, bit_hi, end_word, end_bit, chunk_bits, nchunks, d_first, skip, nullptr, nullptr, 0);
+    return 1;
+}
+
+int launch_find_all(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint64_t end_bit,
+                    uint64_t* out, unsigned* n, unsigned cap, void* stream) {
+    if (bit_hi <= bit_lo + 1) return 0;
+    const uint32_t chunk_bits = 4096 * 8;
+    uint64_t nchunks = (bit_hi - bit_lo + chunk_bits - 1) / chunk_bits;
+    int dev = 0, nsm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    uint64_t blocks = (nchunks + FIND_WARPS - 1) / FIND_WARPS;
+    uint64_t gcap = (uint64_t)nsm * 8;
+    k_find<true><<<(unsigned)(blocks < gcap ? blocks : gcap), FIND_WARPS * 32, 0, (cudaStream_t)stream>>>(
+        (const uint32_t*)d_in, bit_lo, bit_hi, end_word, end_bit, chunk_bits, nchunks, nullptr, nullptr, out, n, cap);
     return 1;
 }
 

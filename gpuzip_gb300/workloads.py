@@ -437,3 +437,101 @@ def zip_archive(entries):
     out += cd
     out += struct.pack("<IHHHHIIH", 0x06054B50, 0, 0, len(entries), len(entries), len(cd), cd_off, 0)
     return bytes(out)
+
+
+# ---------------------------------------------------------------- rescue: a damaged .tar.gz
+
+
+def ustar_header(name, size, mtime=T0):
+    """A POSIX ustar header block (512 bytes) of a regular file."""
+    h = bytearray(512)
+    nb = name.encode()
+    h[0:len(nb)] = nb
+    h[100:108] = b"0000644\0"
+    h[108:116] = b"0001750\0"
+    h[116:124] = b"0001750\0"
+    h[124:136] = b"%011o\0" % size
+    h[136:148] = b"%011o\0" % mtime
+    h[148:156] = b" " * 8
+    h[156:157] = b"0"
+    h[257:263] = b"ustar\0"
+    h[263:265] = b"00"
+    h[148:156] = b"%06o\0 " % sum(h)
+    return bytes(h)
+
+
+def tar_archive(files):
+    """A tar archive (ustar) of (name, bytes) pairs, ended by two zero blocks."""
+    parts = []
+    for name, data in files:
+        parts.append(ustar_header(name, len(data)))
+        parts.append(data)
+        parts.append(bytes(-len(data) % 512))
+    parts.append(bytes(1024))
+    return b"".join(parts)
+
+
+def _file_job(args):
+    seed, index, size, kind = args
+    return stream_content(seed, 1_000_000 + index, size, kind)
+
+
+def _seg_job(args):
+    index, seg, zdict, level, final = args
+    return index, raw_deflate(seg, int(level), zdict=zdict, final=final)
+
+
+def rescue_tar(seed=4, nfiles=2000, lo=4 << 10, hi=8 << 20, workers=None):
+    """(gzip member, info): a .tar.gz of `nfiles` files whose sizes are log-uniform over [lo, hi],
+    each one content kind of the mixed workload (log text 0.50, random 0.20, pattern 0.15,
+    counters 0.15), the tar stream compressed in 1 MiB segments at levels drawn from {1, 6, 9},
+    all in one Deflate stream (as ``mixed_member``). info: crc, size, files [(name, offset in
+    the tar, size)]."""
+    rng = np.random.default_rng([seed, 11])
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), size=nfiles)).astype(np.int64)
+    kinds = rng.choice(4, size=nfiles, p=[0.5, 0.2, 0.15, 0.15])
+    jobs = [(seed, i, int(sizes[i]), int(kinds[i])) for i in range(nfiles)]
+    workers = workers or min(mp.cpu_count(), 32)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        contents = pool.map(_file_job, jobs, chunksize=8)
+    names = [f"data/part{i // 100:02d}/file{i:05d}.bin" for i in range(nfiles)]
+    tar = tar_archive(list(zip(names, contents)))
+    files, off = [], 0
+    for name, data in zip(names, contents):
+        files.append((name, off + 512, len(data)))
+        off += 512 + len(data) + (-len(data) % 512)
+    del contents
+    nseg = (len(tar) + MIB - 1) // MIB
+    levels = rng.choice(np.array([1, 6, 9]), size=nseg)
+    segjobs = [(i, tar[i * MIB:(i + 1) * MIB], tar[max(0, i * MIB - 32768):i * MIB] if i else None, int(levels[i]),
+                i == nseg - 1) for i in range(nseg)]
+    with ctx.Pool(workers) as pool:
+        bodies = pool.map(_seg_job, segjobs, chunksize=4)
+    bodies.sort(key=lambda r: r[0])
+    crc = zlib.crc32(tar)
+    member = gzip_wrap(b"".join(b for _, b in bodies), crc, len(tar))
+    return member, {"crc": crc, "size": len(tar), "files": files}
+
+
+def rescue_damage(member, seed=4, sectors=3, dup=64 << 10, crlf_region=16 << 20):
+    """(damaged copy, what was done): `sectors` 4 KiB sectors zeroed at random 4 KiB-aligned places
+    of the compressed body, one `dup`-byte span written twice (a download resumed at the wrong
+    place), and every CR LF turned into LF inside one `crlf_region`-byte region."""
+    rng = np.random.default_rng([seed, 12])
+    b = bytearray(member)
+    lo, hi = 10, len(b) - 8
+    done = {"sectors": [], "dup": None, "crlf": None}
+    for _ in range(sectors):
+        s = int(rng.integers(lo // 4096 + 1, hi // 4096 - 1)) * 4096
+        b[s:s + 4096] = bytes(4096)
+        done["sectors"].append(s)
+    d = int(rng.integers(lo, hi - dup))
+    b[d + dup:d + dup] = b[d:d + dup]
+    done["dup"] = d
+    r = int(rng.integers(lo, max(lo + 1, len(b) - 8 - crlf_region)))
+    region = bytes(b[r:r + crlf_region])
+    fixed = region.replace(b"\r\n", b"\n")
+    b[r:r + crlf_region] = fixed
+    done["crlf"] = [r, len(region) - len(fixed)]
+    return bytes(b), done

@@ -1,0 +1,113 @@
+/* gzrescue_gb300.h - recovery of damaged gzip data on the GPU: the gr_* entry points of
+ * libgpuinflate.so, with the interface of gzrescue's libgzrescue (interface version 4).
+ *
+ * The names, argument meanings, return codes and struct layouts are those of gzrescue's
+ * gpuinflate/rescue.h:38-107, so that gpuzip's Rust host (src/rescue.rs:193-261) binds these
+ * symbols unchanged; the layouts are part of that interface and are kept field for field.
+ *
+ * What differs is where the work runs: every block header of the file is found and every block
+ * decoded on the GPU at once (one decode from each header, landing on the next), the decisions
+ * of a pass are made on the host from those results, and the bytes, their certainty and the
+ * CRC-32 checks are computed on the GPU. The calls take no context: the library keeps one
+ * device (GPUZIP_RESCUE_DEVICE, default 0) and serializes the calls of a process.
+ *
+ * Not done here (the call behaves as with the option that turns it off): inferring the values
+ * of bytes copied from lost windows (gr_options.no_infer is taken as 1: inferred_bytes is 0),
+ * the search for the CRs a Windows-to-Unix transfer removed from a raw stream with its own CRC
+ * (cr_restored is 0), the one-flipped-bit test for bit rot (it changes only hidden_damage and a
+ * note) and the restart inside a fixed-Huffman block when no block header is left. */
+#ifndef GZRESCUE_GB300_H
+#define GZRESCUE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(GI_BUILD) && defined(__GNUC__)
+#define GR_API __attribute__((visibility("default")))
+#else
+#define GR_API
+#endif
+
+/* reference: gpuinflate/rescue.h:38 */
+#define GR_ABI_VERSION 4
+
+/* Return codes and per-byte certainty. reference: gpuinflate/rescue.h:40-43 (same values) */
+enum { GR_OK = 0, GR_ERR_NO_DEFLATE = 1, GR_ERR_ABORTED = 2, GR_ERR_ARG = 3, GR_ERR_MEMORY = 4, GR_ERR_TOO_BIG = 5, GR_ERR_INTERNAL = 6 };
+enum { GR_UNKNOWN = 0, GR_EXACT = 1, GR_SUSPECT = 2, GR_INFERRED = 3 };
+
+/* reference: gpuinflate/rescue.h:45-56. A field is read only when `size` covers it. */
+typedef struct {
+    uint32_t size;         /* sizeof(gr_options) */
+    uint8_t fill;          /* written where a byte is unknown */
+    uint8_t no_infer;      /* taken as 1 (inference is not done) */
+    uint8_t cr_lost;       /* CR LF to LF transfer: 0 tell from the data, 1 it happened, 2 never */
+    uint8_t crs_expected;  /* raw streams with cr_lost 1: CRs lost, when known (the search is not done) */
+    uint64_t max_output;   /* GR_ERR_TOO_BIG when the output would exceed it; 0: no limit */
+    uint64_t cr_budget;    /* input bytes the CR search may decode (the search is not done) */
+} gr_options;
+
+/* One piece of the output. reference: gpuinflate/rescue.h:58-66 */
+typedef struct {
+    uint64_t out_offset, length; /* in the output */
+    uint64_t decoded, known;     /* bytes the decode produced, of which not unknown */
+    uint64_t in_byte_start, in_byte_end;
+    int32_t suspect;             /* 1: a damaged block */
+    int32_t status;              /* how its decode ended: 0 ok, 1 invalid data, 3 end of input, 4 stopped */
+    uint32_t blocks, symbols;
+    const char* why;             /* suspect: how the damage showed; else "" */
+} gr_piece;
+
+/* reference: gpuinflate/rescue.h:68-86 */
+typedef struct {
+    uint64_t input_size, output_size;
+    uint64_t exact_bytes, suspect_bytes, unknown_bytes;
+    uint32_t headers, pieces, damaged, members;
+    int32_t crc_check;     /* 1 ok, 0 mismatch, -1 not checkable */
+    int64_t length_off;    /* output length minus the trailer's, every block in step; else 0 */
+    int32_t truncated;     /* the file ends inside the stream */
+    int32_t header_damaged;
+    uint64_t input_end;    /* byte after the last decoded block of the first member */
+    uint64_t inferred_bytes;
+    int32_t ascii_undone;  /* an LF to CR LF transfer was undone */
+    uint32_t cr_restored;
+    uint64_t cr_decoded;
+    int32_t hidden_damage; /* damage of a kind that can keep the decoder in step, with no CRC to vouch */
+} gr_stats;
+
+/* Receives the output in order, at most 1 MiB at a time, from the calling thread. Nonzero stops.
+ * reference: gpuinflate/rescue.h:87-88 */
+typedef int (*gr_sink)(void* user, const uint8_t* data, const uint8_t* mask, size_t len);
+
+typedef struct gr_result gr_result;
+
+/* reference: gpuinflate/rescue.h:92 */
+GR_API uint32_t gr_abi_version(void);
+
+/* Recovers the gzip data in in[0..size) into the sink; on GR_OK or GR_ERR_ABORTED *result holds the
+ * statistics, the pieces and the notes (free with gr_free). reference: gpuinflate/rescue.h:94-96 */
+GR_API int gr_rescue(const uint8_t* in, uint64_t size, const gr_options* opt, gr_sink sink, void* user, gr_result** result);
+
+/* The same for a raw Deflate stream at in[0] (a ZIP entry); expected_size UINT64_MAX when unknown,
+ * has_crc: expected_crc holds the original's CRC-32. reference: gpuinflate/rescue.h:98-103 */
+GR_API int gr_rescue_raw(const uint8_t* in, uint64_t size, uint64_t expected_size, int has_crc, uint32_t expected_crc,
+                         const gr_options* opt, gr_sink sink, void* user, gr_result** result);
+
+/* reference: gpuinflate/rescue.h:104-107 */
+GR_API const gr_stats* gr_result_stats(const gr_result* r);
+GR_API uint32_t gr_result_pieces(const gr_result* r, const gr_piece** pieces);
+GR_API uint32_t gr_result_notes(const gr_result* r, const char* const** notes);
+GR_API void gr_free(gr_result* r);
+
+/* Added here, no counterpart in the reference: the number of GPU kernels the last gr_rescue or
+ * gr_rescue_raw call of the process launched. */
+GR_API uint64_t gr_last_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,49 @@
+"""GPU: the rescue path (gr_rescue / gr_rescue_raw of libgpuinflate) against the reference's
+own results on the same damaged inputs (tests/golden/rescue_golden.json, made by gzrescue's
+rescue.cpp with no_infer = 1): the output bytes, the per-byte mask, every statistic and every
+piece are the same. hidden_damage is compared too except where the reference's one-flipped-bit
+test is what set it (that test is not done here)."""
+import os
+import sys
+
+import pytest
+
+from gpuzip_gb300 import gzrescue
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_rescue_golden as G  # noqa: E402
+
+BASES, INFO, CASES = G.load_bases()
+
+
+def compare(name, got, ref):
+    diffs = []
+    for k in ("rc", "out_len", "data_sha256", "mask_sha256", "mask_counts"):
+        if got[k] != ref[k]:
+            diffs.append((k, got[k], ref[k]))
+    if (got["stats"] is None) != (ref["stats"] is None):
+        diffs.append(("stats", got["stats"], ref["stats"]))
+    elif ref["stats"]:
+        for k, v in ref["stats"].items():
+            if got["stats"][k] != v:
+                diffs.append(("stats." + k, got["stats"][k], v))
+    if len(got["pieces"]) != len(ref["pieces"]):
+        diffs.append(("pieces", len(got["pieces"]), len(ref["pieces"])))
+    else:
+        for i, (a, b) in enumerate(zip(got["pieces"], ref["pieces"])):
+            for k in b:
+                if a[k] != b[k]:
+                    diffs.append((f"piece[{i}].{k}", a[k], b[k]))
+    return diffs
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_rescue_matches_reference(case):
+    _, r = G.run_case(case["name"], case["base"], [tuple(o) for o in case["ops"]], BASES, INFO, None)
+    got = G.describe(r)
+    diffs = compare(case["name"], got, case["reference"])
+    assert not diffs, diffs[:12]
+    assert got["largest_chunk"] <= 1 << 20
