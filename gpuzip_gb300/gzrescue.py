@@ -13,7 +13,9 @@ GR_OK, GR_ERR_NO_DEFLATE, GR_ERR_ABORTED, GR_ERR_ARG, GR_ERR_MEMORY, GR_ERR_TOO_
 GR_UNKNOWN, GR_EXACT, GR_SUSPECT, GR_INFERRED = range(4)
 
 EXPORTED = ("gr_abi_version", "gr_rescue", "gr_rescue_raw", "gr_result_stats", "gr_result_pieces", "gr_result_notes",
-            "gr_free", "gr_last_launches")
+            "gr_free", "gr_last_launches", "gr_rescue_tar", "gr_tar_result_stats", "gr_tar_result_files",
+            "gr_tar_result_skipped", "gr_tar_free")
+TAR_INTACT, TAR_SUSPECT, TAR_PARTIAL, TAR_INFERRED, TAR_UNVERIFIED = range(5)
 
 
 class Options(ctypes.Structure):  # gpuinflate/rescue.h:45-56
@@ -37,6 +39,18 @@ class Stats(ctypes.Structure):  # gpuinflate/rescue.h:68-86
                 ("header_damaged", ctypes.c_int32), ("input_end", ctypes.c_uint64), ("inferred_bytes", ctypes.c_uint64),
                 ("ascii_undone", ctypes.c_int32), ("cr_restored", ctypes.c_uint32), ("cr_decoded", ctypes.c_uint64),
                 ("hidden_damage", ctypes.c_int32)]
+
+
+class TarStats(ctypes.Structure):  # gzrescue_gb300.h
+    _fields_ = [("intact", ctypes.c_uint64), ("unverified", ctypes.c_uint64), ("repaired", ctypes.c_uint64),
+                ("bytes", ctypes.c_uint64), ("files", ctypes.c_uint32), ("suspect", ctypes.c_uint32),
+                ("inferred", ctypes.c_uint32), ("partial", ctypes.c_uint32), ("skipped", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32)]
+
+
+class TarFile(ctypes.Structure):  # gzrescue_gb300.h
+    _fields_ = [("name", ctypes.c_char_p), ("offset", ctypes.c_uint64), ("size", ctypes.c_uint64),
+                ("status", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_uint8),
@@ -74,6 +88,18 @@ def bind(path):
     lib.gr_free.restype = None
     if hasattr(lib, "gr_last_launches"):
         lib.gr_last_launches.restype = ctypes.c_uint64
+    if hasattr(lib, "gr_rescue_tar"):
+        lib.gr_rescue_tar.argtypes = [ctypes.c_char_p, u64, ctypes.POINTER(Options), SINK, vp, ctypes.POINTER(vp),
+                                      ctypes.POINTER(vp)]
+        lib.gr_rescue_tar.restype = ctypes.c_int
+        lib.gr_tar_result_stats.argtypes = [vp]
+        lib.gr_tar_result_stats.restype = ctypes.POINTER(TarStats)
+        lib.gr_tar_result_files.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(TarFile))]
+        lib.gr_tar_result_files.restype = ctypes.c_uint32
+        lib.gr_tar_result_skipped.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(u64))]
+        lib.gr_tar_result_skipped.restype = ctypes.c_uint32
+        lib.gr_tar_free.argtypes = [vp]
+        lib.gr_tar_free.restype = None
     _libs[path] = lib
     return lib
 
@@ -120,3 +146,36 @@ def rescue(data, raw=False, expected_size=None, expected_crc=None, fill=0, no_in
         r["notes"] = [nn[i].decode("utf-8", "replace") for i in range(k)]
         lib.gr_free(res)
     return r
+
+
+def rescue_tar(data, fill=0, lib_path=None):
+    """gr_rescue_tar: the rescue (no sink) and the tar walk on the GPU. Returns rc, the rescue's
+    stats, and the file list as the oracle of the reader gives it: intact (count), unverified
+    (count), suspect / inferred / partial (names in archive order), skipped [(offset, bytes)],
+    repaired and bytes, plus every file with its status."""
+    lib = bind(lib_path or gpuinflate.LIB_PATH)
+    opt = Options(ctypes.sizeof(Options), fill, 1, 0, 0, 0, 0)
+    res, tar = ctypes.c_void_p(), ctypes.c_void_p()
+    rc = lib.gr_rescue_tar(bytes(data), len(data), ctypes.byref(opt), SINK(), None, ctypes.byref(res), ctypes.byref(tar))
+    out = {"rc": rc, "stats": None, "tar": None}
+    if res.value:
+        st = lib.gr_result_stats(res).contents
+        out["stats"] = {f: getattr(st, f) for f in STAT_FIELDS}
+        lib.gr_free(res)
+    if tar.value:
+        ts = lib.gr_tar_result_stats(tar).contents
+        fp = ctypes.POINTER(TarFile)()
+        n = lib.gr_tar_result_files(tar, ctypes.byref(fp))
+        files = [(fp[i].name.decode("utf-8", "replace"), fp[i].offset, fp[i].size, fp[i].status) for i in range(n)]
+        sp = ctypes.POINTER(ctypes.c_uint64)()
+        k = lib.gr_tar_result_skipped(tar, ctypes.byref(sp))
+        skipped = [[sp[2 * i], sp[2 * i + 1]] for i in range(k)]
+        out["tar"] = {
+            "intact": ts.intact, "unverified": ts.unverified,
+            "suspect": [f[0] for f in files if f[3] == TAR_SUSPECT],
+            "inferred": [f[0] for f in files if f[3] == TAR_INFERRED],
+            "partial": [f[0] for f in files if f[3] == TAR_PARTIAL],
+            "skipped": skipped, "repaired": ts.repaired, "bytes": ts.bytes, "files": files,
+        }
+        lib.gr_tar_free(tar)
+    return out

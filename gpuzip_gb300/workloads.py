@@ -442,10 +442,10 @@ def zip_archive(entries):
 # ---------------------------------------------------------------- rescue: a damaged .tar.gz
 
 
-def ustar_header(name, size, mtime=T0):
-    """A POSIX ustar header block (512 bytes) of a regular file."""
+def ustar_header(name, size, mtime=T0, typeflag=b"0"):
+    """A POSIX ustar header block (512 bytes): a regular file, or another type."""
     h = bytearray(512)
-    nb = name.encode()
+    nb = name.encode()[:100]
     h[0:len(nb)] = nb
     h[100:108] = b"0000644\0"
     h[108:116] = b"0001750\0"
@@ -453,7 +453,7 @@ def ustar_header(name, size, mtime=T0):
     h[124:136] = b"%011o\0" % size
     h[136:148] = b"%011o\0" % mtime
     h[148:156] = b" " * 8
-    h[156:157] = b"0"
+    h[156:157] = typeflag
     h[257:263] = b"ustar\0"
     h[263:265] = b"00"
     h[148:156] = b"%06o\0 " % sum(h)
@@ -461,12 +461,27 @@ def ustar_header(name, size, mtime=T0):
 
 
 def tar_archive(files):
-    """A tar archive (ustar) of (name, bytes) pairs, ended by two zero blocks."""
+    """A tar archive (ustar) of (name, bytes) or (name, bytes, "pax") entries, ended by two zero
+    blocks. A name longer than 100 bytes goes in a GNU long-name entry ('L') before its header, or
+    with "pax" in a pax extended header ('x') with a path record."""
     parts = []
-    for name, data in files:
-        parts.append(ustar_header(name, len(data)))
+
+    def add(name, data, typeflag=b"0"):
+        parts.append(ustar_header(name, len(data), typeflag=typeflag))
         parts.append(data)
         parts.append(bytes(-len(data) % 512))
+
+    for entry in files:
+        name, data = entry[0], entry[1]
+        if len(entry) > 2 and entry[2] == "pax":
+            rec = b" path=" + name.encode() + b"\n"
+            n = len(rec) + 1
+            while len(str(n)) + len(rec) != n:
+                n = len(str(n)) + len(rec)
+            add("PaxHeaders/" + name[-80:], str(n).encode() + rec, b"x")
+        elif len(name.encode()) > 100:
+            add("././@LongLink", name.encode() + b"\0", b"L")
+        add(name, data)
     parts.append(bytes(1024))
     return b"".join(parts)
 

@@ -106,6 +106,38 @@ GR_API void gr_free(gr_result* r);
  * gr_rescue_raw call of the process launched. */
 GR_API uint64_t gr_last_launches(void);
 
+/* ---- Added here: the tar walk over the rescued output, on the GPU where it lies.
+ * gpuzip's Rust host reads a rescued .tar.gz with its TarReader (src/rescue.rs:374-829) and then
+ * applies two rules (src/main.rs:546-558): these give the same outcome for the stream gr_rescue
+ * produces, without the output leaving the device. A file's status: 0 intact, 1 suspect (its
+ * bytes lie in flagged blocks, or the next header is not where its size says), 2 partial
+ * (unknown bytes, or cut short), 3 inferred, 4 unverified (intact, but the stream's CRC fails with
+ * nothing to blame, or damage that keeps the decoder in step was seen). */
+typedef struct {
+    uint64_t intact, unverified, repaired, bytes; /* files; headers mended from the one before; file bytes read */
+    uint32_t files, suspect, inferred, partial, skipped;
+    uint32_t pad;
+} gr_tar_stats;
+
+typedef struct {
+    const char* name;
+    uint64_t offset, size; /* its data in the output, and the size its header gives */
+    int32_t status;
+    int32_t pad;
+} gr_tar_file;
+
+typedef struct gr_tar gr_tar;
+
+/* gr_rescue, then the tar walk: on GR_OK *tar holds every regular file in archive order with its
+ * status, and the regions with no readable header (free with gr_tar_free). */
+GR_API int gr_rescue_tar(const uint8_t* in, uint64_t size, const gr_options* opt, gr_sink sink, void* user, gr_result** result,
+                         gr_tar** tar);
+GR_API const gr_tar_stats* gr_tar_result_stats(const gr_tar* t);
+GR_API uint32_t gr_tar_result_files(const gr_tar* t, const gr_tar_file** files);
+/* (offset, bytes) pairs */
+GR_API uint32_t gr_tar_result_skipped(const gr_tar* t, const uint64_t** pairs);
+GR_API void gr_tar_free(gr_tar* t);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,6 +21,8 @@ import zlib
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import tar_oracle  # noqa: E402
 from gpuzip_gb300 import gzrescue  # noqa: E402
 from gpuzip_gb300 import workloads as W  # noqa: E402
 
@@ -47,12 +49,33 @@ def make_bases():
                member(W.log_text(46, 350 << 10, exact=True), 1, 5))
     raw_text = W.log_text(47, 900 << 10, exact=True)
     return {
+        "tar": member(tar_base(), 6, 5),
         "text": member(text, 6, 5),
         "text8": member(W.log_text(48, 1280 << 10, exact=True), 6),
         "mixed": mixed,
         "members": members,
         "raw": deflate(raw_text, 9, 5),
     }, {"raw": {"size": len(raw_text), "crc": zlib.crc32(raw_text)}}
+
+
+def tar_base():
+    """A tar of 48 files of the mixed workload's contents (2-96 KiB), one with a GNU long name and
+    one with a pax path."""
+    import numpy as np
+
+    rng = np.random.default_rng([49, 1])
+    files = []
+    for i in range(48):
+        size = int(np.exp(rng.uniform(np.log(2 << 10), np.log(96 << 10))))
+        kind = int(rng.choice(4, p=[0.5, 0.2, 0.15, 0.15]))
+        name = f"src/mod{i // 8}/file{i:03d}.dat"
+        entry = (name, W.stream_content(49, i, size, kind))
+        if i == 17:
+            entry = ("deep/" + "n" * 120 + f"/file{i:03d}.dat", entry[1])
+        if i == 31:
+            entry = ("pax/" + "p" * 110 + f"/file{i:03d}.dat", entry[1], "pax")
+        files.append(entry)
+    return W.tar_archive(files)
 
 
 def damage(data, ops):
@@ -113,10 +136,26 @@ def cases(bases):
         ("members-clean", "members", []),
         ("members-sector", "members", [("zero", frac("members", 0.55), 4096)]),
         ("members-truncated", "members", [("cut", frac("members", 0.90, 1))]),
+        ("tar-clean", "tar", []),
+        ("tar-sector", "tar", [("zero", frac("tar", 0.45), 4096)]),
+        ("tar-three-sectors", "tar", [("zero", frac("tar", 0.20), 4096), ("zero", frac("tar", 0.50), 4096),
+                                      ("zero", frac("tar", 0.80), 4096)]),
+        ("tar-dup-span", "tar", [("dup", frac("tar", 0.35), 65536)]),
+        ("tar-crlf-region", "tar", [("crlf_to_lf", frac("tar", 0.55), frac("tar", 0.30))]),
+        ("tar-truncated", "tar", [("cut", frac("tar", 0.70, 1))]),
+        ("tar-bit-flip", "tar", [("flip", frac("tar", 0.62, 1) * 8 + 3)]),
         ("raw-clean", "raw", []),
         ("raw-sector", "raw", [("zero", frac("raw", 0.50), 4096)]),
         ("raw-no-trailer-info", "raw", [("zero", frac("raw", 0.60), 4096)]),
     ]
+
+
+def tar_outcome(r):
+    """The recovered-file list of a rescued tar (the oracle's restatement of gpuzip's reader)."""
+    s = r["stats"] or {}
+    o = tar_oracle.untar(r["data"], r["mask"], s.get("crc_check", -1), s.get("damaged", 0), s.get("hidden_damage", 0))
+    o["skipped"] = [list(x) for x in o["skipped"]]
+    return o
 
 
 def describe(r):
@@ -150,7 +189,7 @@ def run_case(name, base_name, ops, bases, info, lib_path):
 
 def load_bases():
     bases = {}
-    for name in ("text", "text8", "mixed", "members", "raw"):
+    for name in ("text", "text8", "mixed", "members", "raw", "tar"):
         with open(os.path.join(BASE_DIR, name + ".bin"), "rb") as f:
             bases[name] = f.read()
     with open(OUT) as f:
@@ -170,8 +209,14 @@ def main():
     for name, base_name, ops in cases(bases):
         _, r = run_case(name, base_name, ops, bases, info, REF_LIB)
         d = describe(r)
+        if base_name == "tar" and r["rc"] == 0:
+            d["tar"] = tar_outcome(r)
         out["cases"].append({"name": name, "base": base_name, "ops": [list(o) for o in ops], "reference": d})
         s = d["stats"] or {}
+        if "tar" in d:
+            t = d["tar"]
+            print(f"    tar: intact {t['intact']} unverified {t['unverified']} suspect {len(t['suspect'])} "
+                  f"inferred {len(t['inferred'])} partial {len(t['partial'])} skipped {t['skipped']} repaired {t['repaired']}")
         print(f"{name:22s} rc {d['rc']} out {d['out_len']:8d} pieces {len(d['pieces']):3d} damaged {s.get('damaged')} "
               f"mask {d['mask_counts']} crc {s.get('crc_check')} hidden {s.get('hidden_damage')}")
     with open(OUT, "w") as f:

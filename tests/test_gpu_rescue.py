@@ -47,3 +47,18 @@ def test_rescue_matches_reference(case):
     diffs = compare(case["name"], got, case["reference"])
     assert not diffs, diffs[:12]
     assert got["largest_chunk"] <= 1 << 20
+
+
+TAR_CASES = [c for c in CASES if "tar" in c["reference"]]
+
+
+@pytest.mark.parametrize("case", TAR_CASES, ids=[c["name"] for c in TAR_CASES])
+def test_tar_walk_matches_reader(case):
+    """gr_rescue_tar's file list (the walk on the GPU) is the one gpuzip's reader gives for the
+    reference's rescued stream (its restatement in oracle/tar_oracle.py, recorded in the fixtures)."""
+    data = G.damage(BASES[case["base"]], [tuple(o) for o in case["ops"]])
+    r = gzrescue.rescue_tar(data)
+    assert r["rc"] == 0
+    want = case["reference"]["tar"]
+    got = {k: r["tar"][k] for k in want}
+    assert got == want

@@ -34,4 +34,7 @@ def test_reference_reproduces_fixtures():
     bases, info, cases = G.load_bases()
     for c in cases:
         _, r = G.run_case(c["name"], c["base"], [tuple(o) for o in c["ops"]], bases, info, G.REF_LIB)
-        assert G.describe(r) == c["reference"], c["name"]
+        d = G.describe(r)
+        if "tar" in c["reference"]:
+            d["tar"] = G.tar_outcome(r)
+        assert d == c["reference"], c["name"]
