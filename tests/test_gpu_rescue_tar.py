@@ -1,0 +1,40 @@
+"""GPU: the full-size damaged .tar.gz (2,000 files of mixed content, 2.2 GB of tar; three zeroed
+sectors, a span written twice, CR LF to LF in a 16 MiB region): the GPU rescue's output, mask,
+statistics and piece records, and the recovered-file list of its tar walk, equal what gzrescue's
+own rescue.cpp and the reader's restatement give (tests/golden/rescue_tar_2000.json). The input
+is generated here; where this host's zlib compresses it to other bytes than the fixture's, the
+test says so and is skipped."""
+import hashlib
+import json
+import os
+import sys
+
+import pytest
+
+from gpuzip_gb300 import gzrescue
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(HERE, "golden"))
+sys.path.insert(0, ROOT)
+import make_rescue_tar_golden as TG  # noqa: E402
+
+
+def test_full_size_tar_rescue_matches_reference():
+    with open(TG.OUT) as f:
+        golden = json.load(f)
+    import bench
+
+    data, _ = bench.rescue_workload(2000)  # cached between this test and the benchmark
+    if hashlib.sha256(data).hexdigest() != golden["input_sha256"]:
+        pytest.skip("the generated input differs from the fixture's (another zlib): nothing to compare")
+    r = gzrescue.rescue(data)
+    got = TG.summary(r, data)
+    del r
+    for k in ("rc", "out_len", "data_sha256", "mask_sha256", "mask_counts", "stats", "pieces_sha256", "largest_chunk"):
+        assert got[k] == golden[k], k
+    t = gzrescue.rescue_tar(data)
+    assert t["rc"] == 0 and t["stats"] == golden["stats"]
+    assert {k: t["tar"][k] for k in golden["tar"]} == golden["tar"]
