@@ -5,6 +5,8 @@
 //  - the admitter moves the head of `waiting` into the device arena as soon as the arena has room
 //    for its whole input (the HBM budget), copies the input there on a stream of its own, and
 //    appends the request to `ready`;
+//  - a rescue thread takes the damaged members queued for recovery (GI_REQ_RESCUE), one at a
+//    time in arrival order, beside the passes;
 //  - each worker owns a decode context (its own stream, pass buffers and pinned output buffer);
 //    whenever it is free it takes every ready request that fits its next pass (in order, up to
 //    max_batch), runs the batched form over their device copies, gives their arena ranges back
@@ -88,14 +90,14 @@ struct gi_server {
 
     std::mutex m;
     std::condition_variable cv;
-    std::deque<Request*> waiting, ready;
+    std::deque<Request*> waiting, ready, rescue;
     uint64_t outstanding = 0;  // submitted, callback not yet returned
     uint32_t running = 0;      // passes running
     double busy_from = 0;
     bool stop = false;
     gi_server_stats st{};
     std::mutex done_m;  // callbacks never run two at once
-    std::thread admitter;
+    std::thread admitter, rescuer;
     std::vector<std::thread> workers;
 
     double now() const { return std::chrono::duration<double>(clk::now() - t0).count(); }
@@ -286,6 +288,37 @@ void work_loop(gi_server* s, int w) {
     }
 }
 
+// the rescue requests, in arrival order (the GPU work of a rescue runs beside the passes)
+void rescue_loop(gi_server* s) {
+    cudaSetDevice(s->cfg.device);
+    std::unique_lock<std::mutex> l(s->m);
+    for (;;) {
+        s->cv.wait(l, [&] { return s->stop || !s->rescue.empty(); });
+        if (s->rescue.empty()) return;
+        Request* r = s->rescue.front();
+        s->rescue.pop_front();
+        r->t_admit = r->t_start = s->now();
+        l.unlock();
+        std::vector<uint8_t> buf;
+        uint64_t out_size = 0;
+        int rc = gz::rescue_for_server(s->cfg.device, r->in, r->size, buf, out_size);
+        gi_result res{r->tag, rc == 0 ? GI_OK : GI_ERR_DATA, 0, rc == 0 ? out_size : 0, r->size, r->t_submit, r->t_admit,
+                      r->t_start, 0, 1, s->cfg.workers};
+        {
+            std::lock_guard<std::mutex> dl(s->done_m);
+            res.t_done = s->now();
+            s->done(s->user, &res, res.status == GI_OK ? buf.data() : nullptr);
+        }
+        l.lock();
+        s->st.completed++;
+        s->st.failed += res.status != GI_OK;
+        s->st.out_bytes += res.out_size;
+        s->outstanding--;
+        delete r;
+        s->cv.notify_all();
+    }
+}
+
 void teardown(gi_server* s) {
     {
         std::lock_guard<std::mutex> l(s->m);
@@ -293,6 +326,7 @@ void teardown(gi_server* s) {
         s->cv.notify_all();
     }
     if (s->admitter.joinable()) s->admitter.join();
+    if (s->rescuer.joinable()) s->rescuer.join();
     for (auto& t : s->workers)
         if (t.joinable()) t.join();
     cudaSetDevice(s->cfg.device);
@@ -384,6 +418,7 @@ GI_API int gi_server_create(const gi_server_config* cfg, gi_done done, void* use
     s->st.device_bytes = ctx_bytes + arena;
     s->st.arena_bytes = arena;
     s->admitter = std::thread(admit_loop, s);
+    s->rescuer = std::thread(rescue_loop, s);
     for (uint32_t w = 0; w < c.workers; w++) s->workers.emplace_back(work_loop, s, (int)w);
     *out = s;
     return GI_OK;
@@ -401,7 +436,8 @@ GI_API int gi_server_submit(gi_server* s, const uint8_t* in, uint64_t in_size, u
     }
     r->alone = r->out_guess + 16 > s->pass_out || in_size + PASS_GAP > s->pass_in || in_size > s->arena.capacity();
     r->t_submit = s->now();
-    s->waiting.push_back(r);
+    if (flags & GI_REQ_RESCUE) s->rescue.push_back(r);
+    else s->waiting.push_back(r);
     s->outstanding++;
     s->st.submitted++;
     s->st.in_bytes += in_size;

@@ -44,6 +44,7 @@ EXPORTED = (
 GI_STREAM_GZIP = 1
 GI_STREAM_CRC = 2
 GI_STREAM_MAPPED = 4
+GI_REQ_RESCUE = 8  # server requests only: a damaged gzip member to recover (output then mask)
 
 
 class Config(ctypes.Structure):
@@ -455,14 +456,19 @@ class Server:
         self.lib = load(path)
         self.results = {}
         self._inputs = {}
+        self._flags = {}
         self._lock = threading.Lock()
         self._next = 0
 
         def _cb(user, rp, data):
             r = rp.contents
             d = r.as_dict()
+            with self._lock:
+                rescued = self._flags.pop(r.tag, 0) & GI_REQ_RESCUE
             if keep_output and data and r.status == GI_OK:
                 d["output"] = ctypes.string_at(data, r.out_size)
+                if rescued:  # the mask follows the output
+                    d["mask"] = ctypes.string_at(data + r.out_size, r.out_size)
             if on_done is not None:
                 try:
                     on_done(d, data)
@@ -497,6 +503,7 @@ class Server:
                 tag = self._next
             self._next = max(self._next, tag) + 1
             self._inputs[tag] = keep
+            self._flags[tag] = flags
         rc = self.lib.gi_server_submit(self.srv, ctypes.c_void_p(ptr), size, flags, expected_crc & 0xFFFFFFFF, tag)
         if rc != GI_OK:
             with self._lock:

@@ -126,3 +126,29 @@ def test_passes_overlap_on_the_gpu():
     assert st["overlapped"] >= 1
     assert any(r[k]["worker"] != r[0]["worker"] and r[k]["t_start"] < r[0]["t_done"] for k in range(1, 9))
     assert min(r[k]["t_done"] for k in range(1, 9)) < r[0]["t_done"]
+
+
+def test_rescue_requests_beside_passes(mix):
+    """A damaged member submitted for rescue (GI_REQ_RESCUE) comes back with the output and mask
+    that gr_rescue gives for it alone, while the other requests decode as usual."""
+    from gpuzip_gb300 import gzrescue
+
+    good = [x for x in mix if x["gzip"] and x["size"] > 256 << 10][:4]
+    bad = W.zero_sector(good[1]["data"], 7, 0)
+    srv = gpuinflate.Server(0, workers=2, hbm_budget=40e9, keep_output=True)
+    for i, x in enumerate(good):
+        srv.submit(x["data"], tag=i)
+    srv.submit(bad, flags=GZIP | gpuinflate.GI_REQ_RESCUE, tag=100)
+    srv.submit(good[0]["data"], flags=GZIP | gpuinflate.GI_REQ_RESCUE, tag=101)  # undamaged: all exact
+    srv.drain()
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(good) + 2 and st["failed"] == 0
+    for i, x in enumerate(good):
+        assert srv.results[i]["output"] == expected(x)
+    alone = gzrescue.rescue(bad)
+    r = srv.results[100]
+    assert r["status"] == 0 and r["output"] == alone["data"] and r["mask"] == alone["mask"]
+    assert r["out_size"] == alone["stats"]["output_size"] and r["crc32"] == 0
+    r = srv.results[101]
+    assert r["output"] == expected(good[0]) and r["mask"] == bytes([gzrescue.GR_EXACT]) * len(r["output"])
