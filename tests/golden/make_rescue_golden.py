@@ -144,6 +144,15 @@ def cases(bases):
         ("tar-crlf-region", "tar", [("crlf_to_lf", frac("tar", 0.55), frac("tar", 0.30))]),
         ("tar-truncated", "tar", [("cut", frac("tar", 0.70, 1))]),
         ("tar-bit-flip", "tar", [("flip", frac("tar", 0.62, 1) * 8 + 3)]),
+        ("text-flip-71", t, [("flip", int(len(bases[t]) * 0.71) * 8 + 3)]),
+        ("text8-flip-27", "text8", [("flip", int(len(bases["text8"]) * 0.27) * 8 + 3)]),
+        ("members-flip-13", "members", [("flip", int(len(bases["members"]) * 0.13) * 8 + 3)]),
+        ("members-flip-27", "members", [("flip", int(len(bases["members"]) * 0.27) * 8 + 3)]),
+        ("members-flip-41", "members", [("flip", int(len(bases["members"]) * 0.41) * 8 + 3)]),
+        ("tar-flip-86", "tar", [("flip", int(len(bases["tar"]) * 0.86) * 8 + 3)]),
+        ("raw-flip-mended-59", "raw", [("flip", 1318077)]),
+        ("raw-flip-mended-84", "raw", [("flip", 1871005)]),
+        ("raw-flip-25", "raw", [("flip", 564093)]),
         ("raw-clean", "raw", []),
         ("raw-sector", "raw", [("zero", frac("raw", 0.50), 4096)]),
         ("raw-no-trailer-info", "raw", [("zero", frac("raw", 0.60), 4096)]),
