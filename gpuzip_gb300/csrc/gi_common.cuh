@@ -51,6 +51,10 @@ struct Job {
     uint32_t flags;     // JOB_CHECK_REFS
 };
 constexpr uint32_t JOB_CHECK_REFS = 1;
+// the job's output is not kept: it writes over its first extent again and again (which must hold
+// DISCARD_EXTENT symbols: a stored block and a match), for decodes only their results are wanted from
+constexpr uint32_t JOB_DISCARD = 2;
+constexpr uint32_t DISCARD_EXTENT = 65536 + 512;
 
 struct JobResult {
     uint64_t end_bit;    // where it stopped

@@ -336,6 +336,7 @@ struct Out {
     uint64_t done;    // symbols in earlier extents
     int ext;          // current extent index
     uint16_t stage;   // this lane's symbol of the current group
+    bool discard;     // JOB_DISCARD: the extent is written over instead of growing
 };
 
 __device__ __forceinline__ void flush_partial(Out& o, int lane) {
@@ -376,6 +377,11 @@ __device__ __forceinline__ void emit_run(Out& o, uint32_t len, uint16_t v, int l
 __device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, int job) {
     int lane = C.lane;
     flush_partial(o, lane);
+    if (o.discard) {  // start the same extent over (it holds DISCARD_EXTENT >= need)
+        o.done += o.op;
+        o.op = 0;
+        return need <= o.cap;
+    }
     uint64_t want = o.cap * 2;
     if (want < (64ull << 10)) want = 64ull << 10;
     if (want > (16ull << 20)) want = 16ull << 20;
@@ -501,6 +507,7 @@ __device__ void decode_job(Ctx& C, int k) {
     o.done = 0;
     o.ext = k;
     o.stage = 0;
+    o.discard = (J.flags & JOB_DISCARD) != 0;
     if (lane == 0) {
         Extent x;
         x.pool_off = J.pool_off;
