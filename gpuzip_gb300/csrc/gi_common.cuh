@@ -134,6 +134,7 @@ struct ProbeArgs {
     int32_t nspans;
     uint32_t lead;      // bits decoded before a point to fall into step
     Start* out;
+    uint32_t attempts;  // restarts one bit later a probe makes before giving up on a point
 };
 
 // a run of the segment's output: pool[src .. src+len) goes to output position dst

@@ -807,7 +807,7 @@ __global__ void __launch_bounds__(NWARPS * 32, 4) k_probe(ProbeArgs a) {
             int final = base_final;
             if (ok) {
                 uint64_t start = at - a.lead > ps.start.bit ? at - a.lead : ps.start.bit;
-                for (int attempt = 0; attempt < 32 && start < at && res.bit == UINT64_MAX; attempt++) {
+                for (uint32_t attempt = 0; attempt < a.attempts && start < at && res.bit == UINT64_MAX; attempt++) {
                     if (!have) {
                         have = block_tables(T, a.in, a.end_word, base_header, base_fixed, lane);
                         if (!have) break;

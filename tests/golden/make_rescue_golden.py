@@ -32,14 +32,14 @@ OUT = os.path.join(HERE, "rescue_golden.json")
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libgzrescue_ref.so")
 
 
-def deflate(data, level, mem_level=8):
+def deflate(data, level, mem_level=8, strategy=zlib.Z_DEFAULT_STRATEGY):
     """Raw Deflate; zlib ends a block every 2^(mem_level + 6) - 1 symbols (16,383 at its default 8)."""
-    c = zlib.compressobj(level, zlib.DEFLATED, -15, mem_level)
+    c = zlib.compressobj(level, zlib.DEFLATED, -15, mem_level, strategy)
     return c.compress(data) + c.flush()
 
 
-def member(data, level, mem_level=8):
-    return W.gzip_wrap(deflate(data, level, mem_level), zlib.crc32(data), len(data))
+def member(data, level, mem_level=8, strategy=zlib.Z_DEFAULT_STRATEGY):
+    return W.gzip_wrap(deflate(data, level, mem_level, strategy), zlib.crc32(data), len(data))
 
 
 def make_bases():
@@ -52,6 +52,7 @@ def make_bases():
         "tar": member(tar_base(), 6, 5),
         "text": member(text, 6, 5),
         "text8": member(W.log_text(48, 1280 << 10, exact=True), 6),
+        "fixed": member(W.log_text(50, 384 << 10, exact=True), 6, 5, zlib.Z_FIXED),
         "mixed": mixed,
         "members": members,
         "raw": deflate(raw_text, 9, 5),
@@ -136,6 +137,11 @@ def cases(bases):
         ("members-clean", "members", []),
         ("members-sector", "members", [("zero", frac("members", 0.55), 4096)]),
         ("members-truncated", "members", [("cut", frac("members", 0.90, 1))]),
+        ("fixed-clean", "fixed", []),
+        ("fixed-sector", "fixed", [("zero", frac("fixed", 0.45), 4096)]),
+        ("fixed-two-sectors", "fixed", [("zero", frac("fixed", 0.20), 4096), ("zero", frac("fixed", 0.70), 4096)]),
+        ("fixed-flip", "fixed", [("flip", int(len(bases["fixed"]) * 0.55) * 8 + 6)]),
+        ("fixed-truncated", "fixed", [("cut", frac("fixed", 0.60, 1) + 77)]),
         ("tar-clean", "tar", []),
         ("tar-sector", "tar", [("zero", frac("tar", 0.45), 4096)]),
         ("tar-three-sectors", "tar", [("zero", frac("tar", 0.20), 4096), ("zero", frac("tar", 0.50), 4096),
@@ -198,7 +204,7 @@ def run_case(name, base_name, ops, bases, info, lib_path):
 
 def load_bases():
     bases = {}
-    for name in ("text", "text8", "mixed", "members", "raw", "tar"):
+    for name in ("text", "text8", "mixed", "members", "raw", "tar", "fixed"):
         with open(os.path.join(BASE_DIR, name + ".bin"), "rb") as f:
             bases[name] = f.read()
     with open(OUT) as f:
