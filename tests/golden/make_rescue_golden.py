@@ -8,10 +8,10 @@ stream). Each case applies a list of damage operations to a base - zeroed sector
 twice, a truncation, a run of 0xFF bytes, one flipped bit, a damaged header, a zero tail, CR LF
 to LF in a region, LF to CR LF everywhere - with `damage()`, a pure-Python function of the
 operations, so the damaged bytes do not depend on the zlib of the machine that checks them.
-For every case the reference's gr_rescue (or gr_rescue_raw), called with no_infer = 1 (the
-inference of lost window bytes is not part of the GPU path), gives: its return code, the SHA-256
-of the output and of the mask, the mask's counts per state, every statistic and every piece
-(all fields but the text of `why`).
+For every case the reference's gr_rescue (or gr_rescue_raw), called with no_infer = 1 and again
+with the inference of lost window bytes on (its default), gives: its return code, the SHA-256 of
+the output and of the mask, the mask's counts per state, every statistic and every piece (all
+fields but the text of `why`).
 """
 import hashlib
 import json
@@ -191,14 +191,14 @@ def describe(r):
     }
 
 
-def run_case(name, base_name, ops, bases, info, lib_path):
+def run_case(name, base_name, ops, bases, info, lib_path, no_infer=True):
     data = damage(bases[base_name], ops)
     if base_name == "raw":
         known = name != "raw-no-trailer-info"
         r = gzrescue.rescue(data, raw=True, expected_size=info["raw"]["size"] if known else None,
-                            expected_crc=info["raw"]["crc"] if known else None, lib_path=lib_path)
+                            expected_crc=info["raw"]["crc"] if known else None, lib_path=lib_path, no_infer=no_infer)
     else:
-        r = gzrescue.rescue(data, lib_path=lib_path)
+        r = gzrescue.rescue(data, lib_path=lib_path, no_infer=no_infer)
     return data, r
 
 
@@ -226,12 +226,16 @@ def main():
         d = describe(r)
         if base_name == "tar" and r["rc"] == 0:
             d["tar"] = tar_outcome(r)
-        out["cases"].append({"name": name, "base": base_name, "ops": [list(o) for o in ops], "reference": d})
+        _, ri = run_case(name, base_name, ops, bases, info, REF_LIB, no_infer=False)
+        di = describe(ri)
+        out["cases"].append({"name": name, "base": base_name, "ops": [list(o) for o in ops], "reference": d,
+                             "reference_infer": di})
         s = d["stats"] or {}
         if "tar" in d:
             t = d["tar"]
             print(f"    tar: intact {t['intact']} unverified {t['unverified']} suspect {len(t['suspect'])} "
                   f"inferred {len(t['inferred'])} partial {len(t['partial'])} skipped {t['skipped']} repaired {t['repaired']}")
+        print(f"{name:22s} inferred {(di['stats'] or {}).get('inferred_bytes')} mask {di['mask_counts']}")
         print(f"{name:22s} rc {d['rc']} out {d['out_len']:8d} pieces {len(d['pieces']):3d} damaged {s.get('damaged')} "
               f"mask {d['mask_counts']} crc {s.get('crc_check')} hidden {s.get('hidden_damage')}")
     with open(OUT, "w") as f:

@@ -49,6 +49,16 @@ def test_rescue_matches_reference(case):
     assert got["largest_chunk"] <= 1 << 20
 
 
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_rescue_with_inference_matches_reference(case):
+    """With the inference of lost window bytes on (the reference's default): the bytes it infers,
+    their mask (GR_INFERRED) and every statistic as the reference's."""
+    _, r = G.run_case(case["name"], case["base"], [tuple(o) for o in case["ops"]], BASES, INFO, None, no_infer=False)
+    got = G.describe(r)
+    diffs = compare(case["name"], got, case["reference_infer"])
+    assert not diffs, diffs[:12]
+
+
 TAR_CASES = [c for c in CASES if "tar" in c["reference"]]
 
 

@@ -38,3 +38,5 @@ def test_reference_reproduces_fixtures():
         if "tar" in c["reference"]:
             d["tar"] = G.tar_outcome(r)
         assert d == c["reference"], c["name"]
+        _, ri = G.run_case(c["name"], c["base"], [tuple(o) for o in c["ops"]], bases, info, G.REF_LIB, no_infer=False)
+        assert G.describe(ri) == c["reference_infer"], c["name"]
