@@ -467,7 +467,7 @@ def run_serve(args, ws, rank, local):
         status = [None] * n
 
         rlib = gzrescue.bind(gpuinflate.LIB_PATH)
-        ropt = gzrescue.Options(ctypes.sizeof(gzrescue.Options), 0, 1, 0, 0, 0, 0)
+        ropt = gzrescue.Options(ctypes.sizeof(gzrescue.Options), 0, 0, 0, 0, 0, 0)  # the default options
         got = [0]
 
         def count(_u, _d, _m, nb):  # the rescue's output reaches the host; only its size is kept
@@ -679,7 +679,7 @@ def run_rescue(args, ws, rank, local):
     pinned.numpy()[:] = np.frombuffer(data, dtype=np.uint8)
     ptr = ctypes.cast(pinned.data_ptr(), ctypes.c_char_p)
     lib = gzrescue.bind(gpuinflate.LIB_PATH)
-    opt = gzrescue.Options(ctypes.sizeof(gzrescue.Options), 0, 1, 0, 0, 0, 0)
+    opt = gzrescue.Options(ctypes.sizeof(gzrescue.Options), 0, 0, 0, 0, 0, 0)  # the default options: inference on
     out_cap = info["size"] + (64 << 20)
     h_out = torch.empty(out_cap, dtype=torch.uint8).pin_memory()
     h_mask = torch.empty(out_cap, dtype=torch.uint8).pin_memory()
@@ -754,7 +754,7 @@ def run_rescue(args, ws, rank, local):
                                "mixed workload, seed 4), the tar stream in 1 MiB segments at levels 1/6/9 in one Deflate stream; "
                                f"{info['size']} bytes of tar, {len(data)} bytes damaged: three 4 KiB sectors zeroed, a 64 KiB "
                                f"span written twice, CR LF to LF in a 16 MiB region ({info['damage']['crlf'][1]} CRs lost)",
-                   "options": "no_infer 1 (the inference of lost window bytes is not done on this path)",
+                   "options": "the default gr_options (the inference of lost window bytes on)",
                    "io": "value: host input (page-locked), output and mask left in device memory (no sink); e2e: every "
                          "output and mask byte delivered to a host sink"},
         "e2e": {"value": round(out / te / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": len(data),
@@ -762,8 +762,8 @@ def run_rescue(args, ws, rank, local):
         "gpu_launches": launches,
         "cpu_baseline": None,
         "cpu_baseline_unavailable": "the reference's rescue library is built from its rescue.cpp, which is not on this host",
-        "result": {k: s[k] for k in ("output_size", "exact_bytes", "suspect_bytes", "unknown_bytes", "headers", "pieces",
-                                     "damaged", "crc_check", "hidden_damage")},
+        "result": {k: s[k] for k in ("output_size", "exact_bytes", "suspect_bytes", "unknown_bytes", "inferred_bytes", "headers",
+                                     "pieces", "damaged", "crc_check", "hidden_damage")},
         "mask_counts": counts,
         "tar": tar,
         "clocks": clocks.summary(),

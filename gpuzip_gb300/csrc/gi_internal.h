@@ -16,7 +16,7 @@ uint64_t gi_pass_capacity(const gi_ctx* g, uint64_t* in_cap);
 
 namespace gz {
 // The request server's rescue (gi_rescue.cu): the gzip member in[0..size) rescued on `device` with
-// inference off; `out` gets the output bytes then as many mask bytes, out_size the output's
+// the default options; `out` gets the output bytes then as many mask bytes, out_size the output's
 // length. Returns a GR_* code.
 int rescue_for_server(int device, const uint8_t* in, uint64_t size, std::vector<uint8_t>& out, uint64_t& out_size);
 }  // namespace gz

@@ -104,7 +104,7 @@ def bind(path):
     return lib
 
 
-def rescue(data, raw=False, expected_size=None, expected_crc=None, fill=0, no_infer=True, cr_lost=0, max_output=0,
+def rescue(data, raw=False, expected_size=None, expected_crc=None, fill=0, no_infer=False, cr_lost=0, max_output=0,
            lib_path=None, keep_output=True):
     """Rescues gzip (or, raw=True, raw Deflate) bytes; returns a dict with rc, data, mask, stats,
     pieces and notes (data and mask empty when keep_output is False)."""
@@ -148,13 +148,13 @@ def rescue(data, raw=False, expected_size=None, expected_crc=None, fill=0, no_in
     return r
 
 
-def rescue_tar(data, fill=0, lib_path=None):
+def rescue_tar(data, fill=0, no_infer=False, lib_path=None):
     """gr_rescue_tar: the rescue (no sink) and the tar walk on the GPU. Returns rc, the rescue's
     stats, and the file list as the oracle of the reader gives it: intact (count), unverified
     (count), suspect / inferred / partial (names in archive order), skipped [(offset, bytes)],
     repaired and bytes, plus every file with its status."""
     lib = bind(lib_path or gpuinflate.LIB_PATH)
-    opt = Options(ctypes.sizeof(Options), fill, 1, 0, 0, 0, 0)
+    opt = Options(ctypes.sizeof(Options), fill, 1 if no_infer else 0, 0, 0, 0, 0)
     res, tar = ctypes.c_void_p(), ctypes.c_void_p()
     rc = lib.gr_rescue_tar(bytes(data), len(data), ctypes.byref(opt), SINK(), None, ctypes.byref(res), ctypes.byref(tar))
     out = {"rc": rc, "stats": None, "tar": None}

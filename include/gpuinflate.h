@@ -288,10 +288,10 @@ GI_API int gi_server_create(const gi_server_config* cfg, gi_done done, void* use
                             size_t err_len);
 /* Queues one request; `in` (host memory) must stay valid until its callback has returned.
  * flags: GI_STREAM_GZIP (one gzip member) or GI_STREAM_CRC (raw Deflate with a known CRC-32) or
- * 0 (raw Deflate); or GI_REQ_RESCUE: a damaged gzip member to recover (gzrescue_gb300.h, with
- * inference off), served in arrival order beside the passes; its callback gets status GI_OK when
- * the rescue gave a result (else GI_ERR_DATA), out_size output bytes followed by out_size mask
- * bytes (GR_UNKNOWN / GR_EXACT / GR_SUSPECT), and crc32 0. A rescue's device memory is taken for
+ * 0 (raw Deflate); or GI_REQ_RESCUE: a damaged gzip member to recover (gzrescue_gb300.h, default
+ * options), served in arrival order beside the passes; its callback gets status GI_OK when the
+ * rescue gave a result (else GI_ERR_DATA), out_size output bytes followed by out_size mask bytes
+ * (GR_UNKNOWN / GR_EXACT / GR_SUSPECT / GR_INFERRED), and crc32 0. A rescue's device memory is taken for
  * the request and given back, outside hbm_budget.
  * Returns GI_OK, or GI_ERR_ARG (no input, or the server is shutting down). */
 #define GI_REQ_RESCUE 8

@@ -7,15 +7,13 @@
  *
  * What differs is where the work runs: every block header of the file is found and every block
  * decoded on the GPU at once (one decode from each header, landing on the next), the decisions
- * of a pass are made on the host from those results, and the bytes, their certainty and the
- * CRC-32 checks are computed on the GPU. The calls take no context: the library keeps one
- * device (GPUZIP_RESCUE_DEVICE, default 0) and serializes the calls of a process.
+ * of a pass are made on the host from those results, and the bytes, their certainty, the CRC-32
+ * checks, the one-flipped-bit trials and the scoring of lost window bytes are computed on the GPU.
+ * The calls take no context: the library keeps one device (GPUZIP_RESCUE_DEVICE, default 0) and
+ * serializes the calls of a process.
  *
- * Not done here (the call behaves as with the option that turns it off): inferring the values
- * of bytes copied from lost windows (gr_options.no_infer is taken as 1: inferred_bytes is 0),
- * the search for the CRs a Windows-to-Unix transfer removed from a raw stream with its own CRC
- * (cr_restored is 0), the one-flipped-bit test for bit rot (it changes only hidden_damage and a
- * note) and the restart inside a fixed-Huffman block when no block header is left. */
+ * Not done here (the call behaves as with the option that turns it off): the search for the CRs
+ * a Windows-to-Unix transfer removed from a raw stream with its own CRC (cr_restored is 0). */
 #ifndef GZRESCUE_GB300_H
 #define GZRESCUE_GB300_H
 
@@ -43,7 +41,7 @@ enum { GR_UNKNOWN = 0, GR_EXACT = 1, GR_SUSPECT = 2, GR_INFERRED = 3 };
 typedef struct {
     uint32_t size;         /* sizeof(gr_options) */
     uint8_t fill;          /* written where a byte is unknown */
-    uint8_t no_infer;      /* taken as 1 (inference is not done) */
+    uint8_t no_infer;      /* 1: leave the bytes copied from lost data unknown, do not infer them */
     uint8_t cr_lost;       /* CR LF to LF transfer: 0 tell from the data, 1 it happened, 2 never */
     uint8_t crs_expected;  /* raw streams with cr_lost 1: CRs lost, when known (the search is not done) */
     uint64_t max_output;   /* GR_ERR_TOO_BIG when the output would exceed it; 0: no limit */

@@ -4,7 +4,8 @@ region: gpuzip_gb300.workloads.rescue_tar + rescue_damage, seed 4).
 
     python tests/golden/make_rescue_tar_golden.py      (needs oracle/_ref/libgzrescue_ref.so)
 
-Records the input's SHA-256, and what gzrescue's own rescue.cpp (no_infer = 1) gives: SHA-256 of
+Records the input's SHA-256, and what gzrescue's own rescue.cpp gives, with no_infer = 1 and
+again with inference on (under "infer"): SHA-256 of
 the output and of the mask, the mask counts, every statistic, the SHA-256 of the piece records
 (as JSON, `why` left out), and the recovered-file list the reader's restatement
 (oracle/tar_oracle.py) reads from that output. Takes a few minutes of CPU."""
@@ -41,11 +42,20 @@ def summary(r, data):
 def main():
     data = damaged_input()
     t = time.time()
-    r = gzrescue.rescue(data, lib_path=G.REF_LIB)
+    r = gzrescue.rescue(data, lib_path=G.REF_LIB, no_infer=True)
     secs = time.time() - t
     d = summary(r, data)
     d["tar"] = G.tar_outcome(r)
     d["reference_seconds"] = round(secs, 1)
+    del r
+    # the same with the inference of lost window bytes on (the reference's default)
+    t = time.time()
+    ri = gzrescue.rescue(data, lib_path=G.REF_LIB, no_infer=False)
+    secs_i = time.time() - t
+    di = summary(ri, data)
+    di["tar"] = G.tar_outcome(ri)
+    di["reference_seconds"] = round(secs_i, 1)
+    d["infer"] = di
     with open(OUT, "w") as f:
         json.dump(d, f, indent=1)
     print(json.dumps({k: v for k, v in d.items() if k != "tar"}, indent=1))

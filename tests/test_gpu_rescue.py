@@ -67,7 +67,7 @@ def test_tar_walk_matches_reader(case):
     """gr_rescue_tar's file list (the walk on the GPU) is the one gpuzip's reader gives for the
     reference's rescued stream (its restatement in oracle/tar_oracle.py, recorded in the fixtures)."""
     data = G.damage(BASES[case["base"]], [tuple(o) for o in case["ops"]])
-    r = gzrescue.rescue_tar(data)
+    r = gzrescue.rescue_tar(data, no_infer=True)
     assert r["rc"] == 0
     want = case["reference"]["tar"]
     got = {k: r["tar"][k] for k in want}

@@ -30,11 +30,18 @@ def test_full_size_tar_rescue_matches_reference():
     data, _ = bench.rescue_workload(2000)  # cached between this test and the benchmark
     if hashlib.sha256(data).hexdigest() != golden["input_sha256"]:
         pytest.skip("the generated input differs from the fixture's (another zlib): nothing to compare")
-    r = gzrescue.rescue(data)
+    r = gzrescue.rescue(data, no_infer=True)
     got = TG.summary(r, data)
     del r
     for k in ("rc", "out_len", "data_sha256", "mask_sha256", "mask_counts", "stats", "pieces_sha256", "largest_chunk"):
         assert got[k] == golden[k], k
-    t = gzrescue.rescue_tar(data)
+    t = gzrescue.rescue_tar(data, no_infer=True)
     assert t["rc"] == 0 and t["stats"] == golden["stats"]
     assert {k: t["tar"][k] for k in golden["tar"]} == golden["tar"]
+    if "infer" in golden:  # inference on: the bytes it infers, their mask and the file list
+        gi = golden["infer"]
+        r = gzrescue.rescue(data, no_infer=False)
+        got = TG.summary(r, data)
+        del r
+        for k in ("rc", "out_len", "data_sha256", "mask_sha256", "mask_counts", "stats", "pieces_sha256"):
+            assert got[k] == gi[k], "infer " + k

@@ -146,7 +146,7 @@ def test_rescue_requests_beside_passes(mix):
     assert st["completed"] == len(good) + 2 and st["failed"] == 0
     for i, x in enumerate(good):
         assert srv.results[i]["output"] == expected(x)
-    alone = gzrescue.rescue(bad)
+    alone = gzrescue.rescue(bad)  # the default options, as the server's
     r = srv.results[100]
     assert r["status"] == 0 and r["output"] == alone["data"] and r["mask"] == alone["mask"]
     assert r["out_size"] == alone["stats"]["output_size"] and r["crc32"] == 0
