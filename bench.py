@@ -219,7 +219,7 @@ def run_batch(args, ws, rank, local):
     g = gpuinflate.Gpu(local, segment_out_mb=args.seg_out_mb)
     lib = g.lib
     n = len(streams)
-    # every stream in one pinned host buffer (pageable inputs are copied by the driver at host
+    # every stream in one pinned host buffer (pageable inputs are staged by CUDA at host
     # memcpy speed, which would time the host's memory, not the decode)
     import numpy as np
 

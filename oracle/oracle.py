@@ -14,10 +14,15 @@ _lib = None
 _ref = None
 
 
+def reference_tree():
+    """Where the reference tree is looked for (GI_REFERENCE_DIR, else the build container's copy)."""
+    return os.environ.get("GI_REFERENCE_DIR", "/root/reference")
+
+
 def build(reference_dir=None):
     """Builds liboracle.so (always) and _ref/ (when the reference tree is present)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    ref = reference_dir or os.environ.get("GI_REFERENCE_DIR", "/root/reference")
+    ref = reference_dir or reference_tree()
     if os.path.isdir(os.path.join(ref, "gpuinflate")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True)
 
