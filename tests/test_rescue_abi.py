@@ -71,6 +71,30 @@ def test_struct_layouts():
         assert layout(REF_HEADER) == mine
 
 
+TAR_PROBE = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include HEADER
+int main(void) {
+    printf("%zu %zu %zu %zu %zu\n", sizeof(gr_tar_stats), sizeof(gr_tar_file), offsetof(gr_tar_stats, files),
+           offsetof(gr_tar_file, offset), offsetof(gr_tar_file, status));
+    return 0;
+}
+"""
+
+
+def test_tar_struct_layouts():
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "probe.c")
+        with open(src, "w") as f:
+            f.write(TAR_PROBE.replace("HEADER", '"' + os.path.join(ROOT, "include", "gzrescue_gb300.h") + '"'))
+        exe = os.path.join(d, "probe")
+        subprocess.run(["gcc", "-o", exe, src], check=True)
+        got = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == [ctypes.sizeof(gzrescue.TarStats), ctypes.sizeof(gzrescue.TarFile), gzrescue.TarStats.files.offset,
+                   gzrescue.TarFile.offset.offset, gzrescue.TarFile.status.offset]
+
+
 def test_bad_arguments_without_gpu(lib):
     res = ctypes.c_void_p(1)
     rc = lib.gr_rescue(None, 5, None, gzrescue.SINK(), None, ctypes.byref(res))
@@ -80,3 +104,9 @@ def test_bad_arguments_without_gpu(lib):
     assert lib.gr_result_pieces(None, None) == 0 and lib.gr_result_notes(None, None) == 0
     assert not lib.gr_result_stats(None)
     lib.gr_free(None)
+    tar = ctypes.c_void_p(1)
+    rc = lib.gr_rescue_tar(None, 5, None, gzrescue.SINK(), None, ctypes.byref(res), ctypes.byref(tar))
+    assert rc == gzrescue.GR_ERR_ARG and not tar.value
+    assert lib.gr_tar_result_files(None, None) == 0 and lib.gr_tar_result_skipped(None, None) == 0
+    assert not lib.gr_tar_result_stats(None)
+    lib.gr_tar_free(None)
