@@ -5,7 +5,8 @@
 Workload (seeded, synthetic): one gzip member of 4096 segments of 1 MiB (4 GiB of output, the
 trailer's ISIZE wraps to 0), each segment log text / random bytes / repeated patterns with 1%
 flips / uint32 counters (p = 0.5/0.2/0.15/0.15), each at a zlib level drawn from {1, 6, 9}, all
-in ONE Deflate stream (gpuzip_gb300/workloads.py:mixed_member).
+in ONE Deflate stream written by zlib's deflate with the level changed by deflateParams (no sync
+flush, no empty stored blocks; gpuzip_gb300/workloads.py:mixed_member).
 
 One step = one full decode of the stream. `value`: the compressed stream already in GPU memory,
 the output written to GPU memory (gi_inflate_device), timed with CUDA events around each call
@@ -41,7 +42,7 @@ def workload(seed, nseg):
     from gpuzip_gb300 import workloads as W
 
     os.makedirs(CACHE, exist_ok=True)
-    path = os.path.join(CACHE, f"mixed_s{seed}_n{nseg}.gz")
+    path = os.path.join(CACHE, f"mixed_params_s{seed}_n{nseg}.gz")
     meta = path + ".json"
     if os.path.exists(path) and os.path.exists(meta):
         with open(meta) as f:
@@ -774,7 +775,7 @@ def run_rescue(args, ws, rank, local):
 
 def config_of(args, info):
     return {"workload": f"one gzip member, {args.nseg} x 1 MiB segments of mixed content (seed {args.seed}), levels 1/6/9 "
-                        "in one Deflate stream",
+                        "changed by deflateParams inside one Deflate stream (no sync flush)",
             "output_bytes": info["size"], "compressed_bytes": info["deflate_size"],
             "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"}
 

@@ -50,8 +50,8 @@ def build(verbose=False, ptxas_info=False):
             if log:
                 print(log, file=sys.stderr)
     objs = [o for o, _ in results]
-    r = subprocess.run([cc, "-shared", "-o", OUT] + objs + ARCH + ["-cudart", "static", "-Xcompiler", "-fPIC"],
-                       capture_output=True, text=True)
+    link = ["-cudart", "static", "-Xcompiler", "-fPIC", "-Xlinker", "--version-script=" + os.path.join(CSRC, "exports.map")]
+    r = subprocess.run([cc, "-shared", "-o", OUT] + objs + ARCH + link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     return OUT

@@ -225,9 +225,17 @@ int resolve_setup();  // once per device: kernel attributes (returns a cudaError
 uint64_t resolve_map_slots(uint64_t seg_out_max);  // extra 16-bit slots out16 needs after the output
 int launch_next_window(const uint8_t* out, uint64_t total, const uint8_t* old, uint32_t W, uint8_t* nw, uint32_t newW,
                        void* stream);
+// CRC-32 of data[0..n) into *result: returns the kernels launched, or -1 (nothing launched) when
+// scratch_words words of scratch are fewer than crc_scratch_words(n)
 int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
                 void* stream);
 uint64_t crc_scratch_words(uint64_t n);
+// loads launch_crc's kernels on the current device now (a cudaError_t), so that a later launch_crc
+// takes no device memory for them under lazy module loading
+int crc_prepare();
+
+// the current device's SM count (queried once per device)
+int sm_count();
 // CRC-32 of each of nstreams streams laid out as spans (stream s: spans first_span[s] .. + span_count[s])
 int launch_crc_streams(const uint8_t* data, const SpanDesc* spans, uint64_t nspans, uint32_t* span_crc,
                        const uint32_t* first_span, const uint32_t* span_count, uint32_t nstreams, uint32_t* crc,

@@ -309,7 +309,8 @@ int launch_stored_scan(const uint8_t* d_in, uint64_t byte_lo, uint64_t byte_hi, 
     if (byte_hi <= byte_lo) return 0;
     uint64_t words = (byte_hi - byte_lo) / 4 + 2;
     uint64_t blocks = (words + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
+    const uint64_t max_blocks = (uint64_t)sm_count() * 32;
+    if (blocks > max_blocks) blocks = max_blocks;
     k_stored_scan<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>((const uint32_t*)d_in, byte_lo, byte_hi, end_word,
                                                                        end_byte, out, n, cap);
     return 1;

@@ -8,12 +8,15 @@
 // tile of the input and the tree that merges them) is the file-scope array below, which every
 // GPU that loads this library holds until the process exits (about 1 MiB).
 //
-// The array's address, as the GPU sees it, is looked up once per device with that device
-// current; the first call on a device does that look-up, so that first call must come before
-// any stream capture on that device. Every call on a device shares the one array: calls that
-// overlap on the GPU (different host threads, or different streams without ordering between
-// them) race on it and corrupt each other's result. Nothing in the array needs to start at zero:
-// every word a call reads was written earlier in the same call.
+// The first call on a device sets the entry point up there, with that device current: it looks up
+// the array's address as the GPU sees it and loads the CRC kernels. Under CUDA's lazy module
+// loading (the default) that set-up is when the driver places the array and the kernels' code and
+// constants in device memory, so the first call on each device, with size 0 if there is nothing
+// to check yet, must come before the caller reserves the rest of the device's memory, and before
+// any stream capture on that device; later calls take no device memory. Every call on a device
+// shares the one array: calls that overlap on the GPU (different host threads, or different
+// streams without ordering between them) race on it and corrupt each other's result. Nothing in
+// the array needs to start at zero: every word a call reads was written earlier in the same call.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -70,18 +73,25 @@ extern "C" GI_API int gi_crc32_device_noalloc(int device, const void* d_data, ui
     if (e == cudaSuccess) {
         std::lock_guard<std::mutex> lock(g_mutex);
         if (!g_scratch_addr[device]) {
-            // once per device, with the device current: the array's address as the GPU sees it
+            // once per device, with the device current: the array's address as the GPU sees it,
+            // and the CRC kernels loaded
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_crc_scratch);
+            if (e == cudaSuccess) e = (cudaError_t)gz::crc_prepare();
             if (e == cudaSuccess) g_scratch_addr[device] = (uint32_t*)p;
         }
         scratch = g_scratch_addr[device];
     }
+    bool too_big = false;
     if (e == cudaSuccess) {
-        gz::launch_crc((const uint8_t*)d_data, size, scratch, NOALLOC_WORDS - 8, d_crc, stream);
+        too_big = gz::launch_crc((const uint8_t*)d_data, size, scratch, NOALLOC_WORDS, d_crc, stream) < 0;
         e = cudaGetLastError();
     }
     cudaSetDevice(prev);
+    if (too_big) {
+        say(err, err_len, "input larger than the fixed scratch of this entry point");
+        return GI_ERR_ARG;
+    }
     if (e != cudaSuccess) {
         say(err, err_len, cudaGetErrorString(e));
         return GI_ERR_GPU;

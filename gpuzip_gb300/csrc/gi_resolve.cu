@@ -23,6 +23,8 @@
 // computed on the host.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "gi_common.cuh"
 
 namespace gz {
@@ -663,18 +665,39 @@ uint32_t crc32_combine_host(uint32_t crc1, uint32_t crc2, uint64_t len2) {
     return mulmod_host(crc1, x8n_host(len2)) ^ crc2;
 }
 
+// words launch_crc writes: one CRC per 4 KiB tile, then one per 1024 of the level below until one
+// is left
 uint64_t crc_scratch_words(uint64_t n) {
-    uint64_t t = n / 4096;
-    uint64_t total = 0;
-    while (t > 1) {
-        total += t;
-        t = (t + 1023) / 1024;
+    uint64_t level = n / 4096, words = level;
+    while (level > 1) {
+        level = (level + 1023) / 1024;
+        words += level;
     }
-    return total + 4;
+    return words + 4;
+}
+
+int crc_prepare() {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_crc_tiles);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_crc_merge);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_crc_tail);
+    return (int)e;
+}
+
+int sm_count() {
+    static std::atomic<int> counts[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+    if (dev < 64 && counts[dev].load(std::memory_order_relaxed) > 0) return counts[dev].load(std::memory_order_relaxed);
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+    if (dev < 64) counts[dev].store(n, std::memory_order_relaxed);
+    return n;
 }
 
 int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scratch_words, uint32_t* result,
                void* stream) {
+    if (scratch_words < crc_scratch_words(n)) return -1;
     int launches = 1;
     cudaStream_t st = (cudaStream_t)stream;
     CrcConsts k{};
@@ -685,7 +708,8 @@ int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scra
     uint64_t item = 4096;
     if (ntiles) {
         unsigned grid = (unsigned)((ntiles + 7) / 8);
-        if (grid > 152 * 16) grid = 152 * 16;
+        const unsigned cap = (unsigned)sm_count() * 16;
+        if (grid > cap) grid = cap;
         k_crc_tiles<<<grid, 256, 0, st>>>(data, ntiles, cur, k);
         launches++;
         while (cnt > 1) {
@@ -699,7 +723,6 @@ int launch_crc(const uint8_t* data, uint64_t n, uint32_t* scratch, uint64_t scra
             item *= 1024;
         }
     }
-    (void)scratch_words;
     uint32_t tail = (uint32_t)(n - ntiles * 4096);
     k_crc_tail<<<1, 256, 0, st>>>(data, ntiles * 4096, tail, cur, x8n_host(tail), result);
     return launches;
@@ -740,7 +763,8 @@ __global__ void k_gather(const GatherPiece* __restrict__ pieces, uint64_t n, uin
 
 int launch_gather(const GatherPiece* pieces, uint64_t n, uint8_t* dst, void* stream) {
     if (!n) return 0;
-    uint64_t grid = n < 152 * 8 ? n : 152 * 8;
+    const uint64_t cap = (uint64_t)sm_count() * 8;
+    uint64_t grid = n < cap ? n : cap;
     k_gather<<<(unsigned)grid, 256, 0, (cudaStream_t)stream>>>(pieces, n, dst);
     return 1;
 }
@@ -852,7 +876,8 @@ int launch_crc_streams(const uint8_t* data, const SpanDesc* spans, uint64_t nspa
     CrcConsts k{};
     for (int s = 0; s < 5; s++) k.lane[s] = x8n_host(128ull << s);
     if (nspans) {
-        k_crc_spans<<<(unsigned)(nspans < 152 * 8 ? nspans : 152 * 8), 256, 0, st>>>(data, spans, nspans, span_crc, k,
+        const uint64_t cap = (uint64_t)sm_count() * 8;
+        k_crc_spans<<<(unsigned)(nspans < cap ? nspans : cap), 256, 0, st>>>(data, spans, nspans, span_crc, k,
                                                                                      x8n_host(4096));
         launches++;
     }

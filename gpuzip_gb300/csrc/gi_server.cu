@@ -32,6 +32,7 @@
 #include "gpuinflate.h"
 #include "gi_arena.h"
 #include "gi_internal.h"
+#include "gzrescue_gb300.h"
 
 namespace {
 
@@ -288,6 +289,20 @@ void work_loop(gi_server* s, int w) {
     }
 }
 
+// a rescue's GR_* code as a request status: input with nothing to recover is bad data; running
+// out of memory or an internal failure is the GPU's side (retry later, or elsewhere); an output
+// past its limit is a lack of space
+int rescue_status(int gr) {
+    switch (gr) {
+        case GR_OK: return GI_OK;
+        case GR_ERR_MEMORY:
+        case GR_ERR_INTERNAL: return GI_ERR_GPU;
+        case GR_ERR_TOO_BIG: return GI_ERR_SPACE;
+        case GR_ERR_ARG: return GI_ERR_ARG;
+        default: return GI_ERR_DATA;
+    }
+}
+
 // the rescue requests, in arrival order (the GPU work of a rescue runs beside the passes)
 void rescue_loop(gi_server* s) {
     cudaSetDevice(s->cfg.device);
@@ -302,7 +317,7 @@ void rescue_loop(gi_server* s) {
         std::vector<uint8_t> buf;
         uint64_t out_size = 0;
         int rc = gz::rescue_for_server(s->cfg.device, r->in, r->size, buf, out_size);
-        gi_result res{r->tag, rc == 0 ? GI_OK : GI_ERR_DATA, 0, rc == 0 ? out_size : 0, r->size, r->t_submit, r->t_admit,
+        gi_result res{r->tag, rescue_status(rc), 0, rc == 0 ? out_size : 0, r->size, r->t_submit, r->t_admit,
                       r->t_start, 0, 1, s->cfg.workers};
         {
             std::lock_guard<std::mutex> dl(s->done_m);

@@ -11,14 +11,20 @@ None of the reference's datasets are reproduced: every stream here is generated 
   log text (p=0.50), uniform random bytes (0.20), a 4-64-byte pattern repeated with 1% of its
   bytes replaced at random (0.15), little-endian uint32 counters with small random deltas
   (0.15); each segment compressed at a level drawn from {1, 6, 9}, all inside ONE Deflate
-  stream: every segment is compressed with the previous 32 KiB of output as its preset
-  dictionary and ended with a sync flush, so matches reach across segments and the segments
-  join into one stream (the last one carries the final block). 4096 segments = 4 GiB, whose
-  gzip ISIZE wraps to 0.
+  stream by zlib's own deflate with the level changed by deflateParams between segments (which
+  ends the current block, not byte-aligned, when the match finder changes, and adds no empty
+  stored block). Runs of at least 64 segments are compressed in parallel processes, each with
+  the 32 KiB before it as its preset dictionary; a run ends after a segment of random bytes, whose
+  last 64 KiB go through deflateParams(0) into stored blocks (what zlib writes for random bytes
+  at any level), then a Z_BLOCK flush, so the run ends on a byte boundary and the next run's
+  blocks follow it in place. The stream has no empty stored block or other sync marker. 4096
+  segments = 4 GiB, whose gzip ISIZE wraps to 0.
 * ``fuzz_streams`` - eight small raw streams of every block kind (levels 1/6/9, fixed only,
   stored only, Huffman only, mixed random/text/runs, tiny), the kinds the reference fuzzes
   (gpuinflate/make_fuzz_inputs.py); made from this module's own text.
 """
+import ctypes
+import ctypes.util
 import multiprocessing as mp
 import struct
 import zlib
@@ -205,26 +211,183 @@ def mixed_segment(seed, index, kind, seg_bytes=MIB):
     return vals.astype("<u4").tobytes()
 
 
-def _mixed_job(args):
-    seed, index, nseg, kind, prev_kind, level, seg_bytes = args
-    data = mixed_segment(seed, index, kind, seg_bytes)
-    zdict = mixed_segment(seed, index - 1, prev_kind, seg_bytes)[-32768:] if index > 0 else None
-    body = raw_deflate(data, int(level), zdict=zdict, final=index == nseg - 1)
-    return index, body, zlib.crc32(data), len(data)
+class _ZStream(ctypes.Structure):
+    """zlib's z_stream as its shared library lays it out (LP64: uLong is 64 bits)."""
+
+    _fields_ = [("next_in", ctypes.c_void_p), ("avail_in", ctypes.c_uint), ("total_in", ctypes.c_ulong),
+                ("next_out", ctypes.c_void_p), ("avail_out", ctypes.c_uint), ("total_out", ctypes.c_ulong),
+                ("msg", ctypes.c_char_p), ("state", ctypes.c_void_p), ("zalloc", ctypes.c_void_p),
+                ("zfree", ctypes.c_void_p), ("opaque", ctypes.c_void_p), ("data_type", ctypes.c_int),
+                ("adler", ctypes.c_ulong), ("reserved", ctypes.c_ulong)]
+
+
+_Z = None
+Z_NO_FLUSH, Z_BLOCK_FLUSH, Z_FINISH_FLUSH = 0, 5, 4
+
+
+def _libz():
+    global _Z
+    if _Z is None:
+        z = ctypes.CDLL(ctypes.util.find_library("z") or "libz.so.1")
+        p = ctypes.POINTER(_ZStream)
+        z.zlibVersion.restype = ctypes.c_char_p
+        z.deflateInit2_.argtypes = [p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_char_p, ctypes.c_int]
+        z.deflate.argtypes = [p, ctypes.c_int]
+        z.deflateParams.argtypes = [p, ctypes.c_int, ctypes.c_int]
+        z.deflateSetDictionary.argtypes = [p, ctypes.c_char_p, ctypes.c_uint]
+        z.deflatePending.argtypes = [p, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_int)]
+        z.deflateEnd.argtypes = [p]
+        _Z = z
+    return _Z
+
+
+class Deflater:
+    """One raw Deflate stream written by zlib's deflate through its C interface, for the calls
+    Python's zlib module does not offer: deflateParams (a level change inside the stream) and
+    deflatePending (the bits of the last block still held back after a Z_BLOCK flush)."""
+
+    def __init__(self, level, zdict=None):
+        self.z = _libz()
+        self.s = _ZStream()
+        rc = self.z.deflateInit2_(ctypes.byref(self.s), int(level), 8, -15, 9, 0, self.z.zlibVersion(),
+                                  ctypes.sizeof(_ZStream))
+        if rc != 0:
+            raise RuntimeError(f"deflateInit2 failed: {rc}")
+        self.level = int(level)
+        if zdict:
+            rc = self.z.deflateSetDictionary(ctypes.byref(self.s), zdict, len(zdict))
+            if rc != 0:
+                raise RuntimeError(f"deflateSetDictionary failed: {rc}")
+
+    def _run(self, data, flush):
+        out = []
+        src = ctypes.create_string_buffer(bytes(data), max(1, len(data)))
+        self.s.next_in = ctypes.cast(src, ctypes.c_void_p)
+        self.s.avail_in = len(data)
+        cap = len(data) + (len(data) >> 3) + (64 << 10)
+        while True:
+            buf = ctypes.create_string_buffer(cap)
+            self.s.next_out = ctypes.cast(buf, ctypes.c_void_p)
+            self.s.avail_out = cap
+            rc = self.z.deflate(ctypes.byref(self.s), flush)
+            if rc not in (0, 1, -5):  # Z_OK, Z_STREAM_END, Z_BUF_ERROR (no progress possible)
+                raise RuntimeError(f"deflate failed: {rc}")
+            out.append(buf.raw[:cap - self.s.avail_out])
+            if self.s.avail_out and self.s.avail_in == 0:
+                return b"".join(out)
+
+    def write(self, data):
+        return self._run(data, Z_NO_FLUSH)
+
+    def params(self, level):
+        """A level change, as deflateParams makes it (any output it flushes is returned)."""
+        out = []
+        while True:
+            cap = 1 << 20
+            buf = ctypes.create_string_buffer(cap)
+            self.s.next_in, self.s.avail_in = None, 0
+            self.s.next_out = ctypes.cast(buf, ctypes.c_void_p)
+            self.s.avail_out = cap
+            rc = self.z.deflateParams(ctypes.byref(self.s), int(level), 0)
+            out.append(buf.raw[:cap - self.s.avail_out])
+            if rc == 0:
+                self.level = int(level)
+                return b"".join(out)
+            if rc != -5:
+                raise RuntimeError(f"deflateParams failed: {rc}")
+
+    def end_block(self):
+        """(bytes, bits): the stream so far ended by a Z_BLOCK flush, with the 0-7 bits of its last
+        byte that zlib still holds (the byte is padded with zeros)."""
+        body = self._run(b"", Z_BLOCK_FLUSH)
+        pend, bits = ctypes.c_uint(0), ctypes.c_int(0)
+        self.z.deflatePending(ctypes.byref(self.s), ctypes.byref(pend), ctypes.byref(bits))
+        if pend.value:
+            raise RuntimeError("zlib holds whole bytes after a Z_BLOCK flush")
+        nbits = 8 * len(body) + bits.value
+        if bits.value:
+            # the held bits lead the first byte the final flush writes
+            tail = self._run(b"", Z_FINISH_FLUSH)
+            body += bytes([tail[0] & ((1 << bits.value) - 1)])
+        return body, nbits
+
+    def finish(self):
+        return self._run(b"", Z_FINISH_FLUSH)
+
+    def close(self):
+        self.z.deflateEnd(ctypes.byref(self.s))
+
+
+RUN_SEGMENTS = 64  # segments per compressor process of the mixed workload (at least)
+
+
+def run_bounds(kinds, nseg, every=RUN_SEGMENTS):
+    """Where the mixed workload's compressor runs start: each run ends after a segment of uniform
+    random bytes (whose end is written as stored blocks, so the run ends on a byte boundary and
+    the next run's bits follow it in place), the first such segment once the run has at least
+    `every` segments."""
+    bounds, i = [0], every
+    while i < nseg:
+        j = i - 1
+        while j < nseg - 1 and kinds[j] != KIND_RANDOM:
+            j += 1
+        if j >= nseg - 1:
+            break
+        bounds.append(j + 1)
+        i = j + 1 + every
+    return bounds + [nseg]
+
+
+def _mixed_run(args):
+    """Segments [first, last) compressed as one run of the stream: the preset dictionary is the
+    32 KiB before the run, the level changes by deflateParams, and the run ends with a Z_BLOCK
+    flush right after stored blocks (so on a byte boundary), or with the final block for the last
+    run. (first, bytes, crc, size)."""
+    seed, first, last, nseg, kinds, levels, seg_bytes = args
+    zdict = mixed_segment(seed, first - 1, kinds[first - 1], seg_bytes)[-32768:] if first > 0 else None
+    d = Deflater(levels[first], zdict=zdict)
+    out, crc, size = [], 0, 0
+    for i in range(first, last):
+        if levels[i] != d.level:
+            out.append(d.params(levels[i]))
+        data = mixed_segment(seed, i, kinds[i], seg_bytes)
+        if i == last - 1 and last < nseg:
+            # the run's closing random segment: its last 64 KiB as stored blocks (level 0), as
+            # zlib writes random bytes at any level, so the run ends on a byte boundary
+            cut = max(0, len(data) - (64 << 10))
+            out.append(d.write(data[:cut]))
+            out.append(d.params(0))
+            out.append(d.write(data[cut:]))
+        else:
+            out.append(d.write(data))
+        crc = crc32_combine(crc, zlib.crc32(data), len(data))
+        size += len(data)
+    if last == nseg:
+        out.append(d.finish())
+    else:
+        tail, bits = d.end_block()
+        if bits % 8:
+            raise RuntimeError(f"segments {first}-{last}: the run does not end on a byte boundary")
+        out.append(tail)
+    d.close()
+    return first, b"".join(out), crc, size
 
 
 def mixed_member(seed=2, nseg=4096, seg_bytes=MIB, workers=None, want_raw=False):
     """(gzip member, info) of the mixed workload. info: crc, size, kinds, levels, deflate offset,
     and the raw output when want_raw (only for small nseg)."""
     kinds, levels = mixed_plan(seed, nseg)
-    jobs = [(seed, i, nseg, int(kinds[i]), int(kinds[i - 1]) if i else 0, int(levels[i]), seg_bytes) for i in range(nseg)]
+    kl, ll = [int(k) for k in kinds], [int(v) for v in levels]
+    bounds = run_bounds(kl, nseg)
+    jobs = [(seed, a, b, nseg, kl, ll, seg_bytes) for a, b in zip(bounds[:-1], bounds[1:])]
     workers = workers or min(mp.cpu_count(), 32)
-    if nseg >= 8 and workers > 1:
+    if len(jobs) > 1 and workers > 1:
         ctx = mp.get_context("spawn")
-        with ctx.Pool(workers) as pool:
-            res = pool.map(_mixed_job, jobs, chunksize=max(1, nseg // (workers * 8)))
+        with ctx.Pool(min(workers, len(jobs))) as pool:
+            res = pool.map(_mixed_run, sorted(jobs, key=lambda j: j[1] - j[2]), chunksize=1)
     else:
-        res = [_mixed_job(j) for j in jobs]
+        res = [_mixed_run(j) for j in jobs]
     res.sort(key=lambda r: r[0])
     crc, size = 0, 0
     for _, _, c, n in res:
@@ -232,13 +395,11 @@ def mixed_member(seed=2, nseg=4096, seg_bytes=MIB, workers=None, want_raw=False)
         size += n
     body = b"".join(r[1] for r in res)
     member = gzip_wrap(body, crc, size)
-    info = {"crc": crc, "size": size, "kinds": kinds, "levels": levels, "deflate_offset": 10, "deflate_size": len(body)}
+    info = {"crc": crc, "size": size, "kinds": kinds, "levels": levels, "deflate_offset": 10, "deflate_size": len(body),
+            "runs": len(jobs)}
     if want_raw:
         info["raw"] = b"".join(mixed_segment(seed, i, int(kinds[i]), seg_bytes) for i in range(nseg))
     return member, info
-
-
-# ---------------------------------------------------------------- fuzz inputs
 
 
 def fuzz_streams(seed=7):

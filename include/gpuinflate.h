@@ -166,9 +166,12 @@ GI_API int gi_last_profile(const gi_ctx* ctx, gi_profile* profile);
  * For callers that cannot allocate device memory: it allocates nothing, its scratch is a fixed
  * 1 MiB array that every GPU loading this library holds until the process exits. Limits: at
  * most 1 GiB per call, d_data 16-byte aligned (else GI_ERR_ARG, with the reason in err). The
- * first call on a device looks the array up, so make it before any stream capture on that
- * device; calls that overlap on one device share the array and race. No counterpart in the
- * reference (its CRC is computed on the host by its caller). */
+ * first call on a device sets it up there (looks the array up and loads the CRC kernels); under
+ * CUDA's lazy module loading that is when the driver places the array and the kernels in device
+ * memory, so make that first call (size 0 is enough) before reserving the rest of the device's
+ * memory and before any stream capture on that device; later calls take no device memory. Calls
+ * that overlap on one device share the array and race. No counterpart in the reference (its CRC
+ * is computed on the host by its caller). */
 GI_API int gi_crc32_device_noalloc(int device, const void* d_data, uint64_t size, uint32_t* d_crc, void* stream,
                                    char* err, size_t err_len);
 

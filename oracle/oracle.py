@@ -14,17 +14,31 @@ _lib = None
 _ref = None
 
 
+TREE_NOTE = os.path.join(HERE, "_ref", "TREE")  # where build() last found the reference tree
+
+
 def reference_tree():
-    """Where the reference tree is looked for (GI_REFERENCE_DIR, else the build container's copy)."""
-    return os.environ.get("GI_REFERENCE_DIR", "/root/reference")
+    """The reference source tree: GI_REFERENCE_DIR, else the tree build() last built _ref/ from,
+    else None. Only where that tree exists are the reference's own files compared or built."""
+    env = os.environ.get("GI_REFERENCE_DIR")
+    if env:
+        return env
+    try:
+        with open(TREE_NOTE) as f:
+            return f.read().strip() or None
+    except OSError:
+        return None
 
 
 def build(reference_dir=None):
-    """Builds liboracle.so (always) and _ref/ (when the reference tree is present)."""
+    """Builds liboracle.so (always) and, when `reference_dir` (or GI_REFERENCE_DIR) names a
+    reference tree that exists, _ref/ from it."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    ref = reference_dir or reference_tree()
-    if os.path.isdir(os.path.join(ref, "gpuinflate")):
+    ref = reference_dir or os.environ.get("GI_REFERENCE_DIR")
+    if ref and os.path.isdir(os.path.join(ref, "gpuinflate")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True)
+        with open(TREE_NOTE, "w") as f:
+            f.write(ref)
 
 
 def lib():

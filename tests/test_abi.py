@@ -17,6 +17,11 @@ def declared():
     return set(re.findall(r"GI_API\s+[\w\s\*]+?\b(gi_\w+)\s*\(", src))
 
 
+def declared_rescue():
+    src = open(os.path.join(ROOT, "include", "gzrescue_gb300.h")).read()
+    return set(re.findall(r"GR_API\s+[\w\s\*]+?\b(gr_\w+)\s*\(", src))
+
+
 @pytest.fixture(scope="module")
 def lib():
     if not os.path.exists(gpuinflate.LIB_PATH):
@@ -34,6 +39,19 @@ def test_exports_every_declared_symbol(lib):
     assert names <= exported, names - exported
     assert exported == names, exported - names  # nothing else is exported (visibility hidden)
     assert set(gpuinflate.EXPORTED) == names
+
+
+def test_dynamic_table_holds_only_the_interfaces(lib):
+    """Every defined dynamic symbol of the library is a declared gi_* or gr_* function: no C++
+    runtime instances (std::thread, std::vector of this library's types) leak into the table a
+    host that also links libstdc++ could resolve against."""
+    out = subprocess.run(["nm", "-D", "--defined-only", gpuinflate.LIB_PATH], capture_output=True, text=True).stdout
+    rows = [ln.split() for ln in out.splitlines() if ln.strip()]
+    syms = {r[-1]: r[-2] for r in rows}
+    want = declared() | declared_rescue()
+    assert "gr_rescue" in want and "gr_rescue_raw" in want and "gr_free" in want
+    assert set(syms) == want, (set(syms) - want, want - set(syms))
+    assert all(kind == "T" for kind in syms.values()), syms
 
 
 def test_abi_version(lib):

@@ -1,8 +1,8 @@
 """GPU: the rescue path (gr_rescue / gr_rescue_raw of libgpuinflate) against the reference's
 own results on the same damaged inputs (tests/golden/rescue_golden.json, made by gzrescue's
-rescue.cpp with no_infer = 1): the output bytes, the per-byte mask, every statistic and every
-piece are the same. hidden_damage is compared too except where the reference's one-flipped-bit
-test is what set it (that test is not done here)."""
+rescue.cpp with no_infer = 1 and again with the inference on): the output bytes, the per-byte
+mask, every statistic (hidden_damage included, which the one-flipped-bit test sets) and every
+piece are the same; for the tar cases, the file list of gr_rescue_tar is the reader's."""
 import os
 import sys
 

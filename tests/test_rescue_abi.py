@@ -14,7 +14,7 @@ import oracle
 from gpuzip_gb300 import gpuinflate, gzrescue
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_HEADER = os.path.join(oracle.reference_tree(), "gpuinflate", "rescue.h")
+REF_HEADER = os.path.join(oracle.reference_tree() or "", "gpuinflate", "rescue.h")
 
 PROBE = r"""
 #include <stdio.h>

@@ -54,3 +54,46 @@ def test_noalloc_rejects_what_does_not_fit():
     with pytest.raises(gpuinflate.InflateError) as e:
         gpuinflate.crc32_device_noalloc(d.data_ptr() + 1, 16, d_crc.data_ptr())
     assert e.value.code == gpuinflate.GI_ERR_ARG and "aligned" in e.value.msg
+
+
+SET_UP_THEN_FULL = r"""
+import sys, zlib
+import torch
+sys.path.insert(0, sys.argv[1])
+from gpuzip_gb300 import gpuinflate
+data = bytes(range(256)) * 40000 + b"tail"
+d = torch.frombuffer(bytearray(data), dtype=torch.uint8).cuda()
+d_crc = torch.zeros(1, dtype=torch.int64, device="cuda")
+torch.cuda.synchronize()
+gpuinflate.crc32_device_noalloc(d.data_ptr(), 0, d_crc.data_ptr())  # the set-up call, before the pool
+torch.cuda.synchronize()
+free, _ = torch.cuda.mem_get_info()
+filler = torch.empty(free - (256 << 20), dtype=torch.uint8, device="cuda")  # the caller's pool
+torch.cuda.synchronize()
+before, _ = torch.cuda.mem_get_info()
+for _ in range(2):
+    d_crc.zero_()
+    gpuinflate.crc32_device_noalloc(d.data_ptr(), len(data), d_crc.data_ptr())
+    torch.cuda.synchronize()
+    assert int(d_crc[0].item()) & 0xFFFFFFFF == zlib.crc32(data)
+after, _ = torch.cuda.mem_get_info()
+assert after == before, (before, after)
+print("ok", before >> 20, "MiB free")
+"""
+
+
+def test_noalloc_after_the_device_is_filled():
+    """A fresh process, lazy module loading: the set-up call (size 0) comes first, then the caller
+    takes all but 256 MiB of the device for its own pool; the entry point then computes the CRC-32
+    twice with no change in free device memory."""
+    import os
+    import subprocess
+    import sys
+
+    pytest.importorskip("torch")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, CUDA_MODULE_LOADING="LAZY")
+    r = subprocess.run([sys.executable, "-c", SET_UP_THEN_FULL, root], capture_output=True, text=True, env=env,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok")
