@@ -162,8 +162,12 @@ int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t 
 // in no order (*n counts them all, including those past cap)
 int launch_find_all(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint64_t end_bit,
                     uint64_t* out, unsigned* n, unsigned cap, void* stream);
+// for the block starting at each bits[i]: (output bytes, codes) per compressed bit, predicted
+// from its header's code lengths ((0, 0) for UINT64_MAX or no valid header)
+int launch_density(const uint8_t* d_in, uint64_t end_word, const uint64_t* bits, uint64_t n, float2* out, void* stream);
 int launch_stored_scan(const uint8_t* d_in, uint64_t byte_lo, uint64_t byte_hi, uint64_t end_word, uint64_t end_byte,
                        StoredCand* out, unsigned* n, unsigned cap, void* stream);
+constexpr int DECODE_WARPS = 8;  // decoders (warps) per block of k_decode
 int decode_blocks_per_sm();
 int launch_decode(const DecodeArgs& a, int grid, void* stream);
 int launch_probe(const ProbeArgs& a, int grid, void* stream);

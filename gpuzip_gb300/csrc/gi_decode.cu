@@ -30,7 +30,7 @@ namespace gz {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int NWARPS = 8;  // decoders per block
+constexpr int NWARPS = DECODE_WARPS;  // decoders per block
 constexpr int LB = 10;     // literal/length lookup bits
 constexpr int DB = 8;      // distance lookup bits
 constexpr int CB = 7;      // code-length code lookup bits (its codes are at most 7 bits)

@@ -302,7 +302,121 @@ __global__ void k_stored_scan(const uint32_t* __restrict__ w, uint64_t byte_lo, 
     }
 }
 
+// ---------------------------------------------------------------- block density
+//
+// How many output bytes and how many codes a block yields per compressed bit, predicted from its
+// header alone: a Huffman code of length L is taken to occur with probability 2^-L, so a dynamic
+// block yields E[output] / E[bits] bytes and 1 / E[bits] codes per bit, a match's bits including
+// its length's extra bits and its distance code's average cost. The planner prices a decoder's
+// job from them (its time follows the codes it decodes and, less, the bytes it writes), and
+// places no probe points in a block whose codes barely compress (a near-flat code: a decode
+// started off the symbol boundaries does not fall back onto them).
+
+__device__ const uint16_t c_len_base[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                                            31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+__device__ const uint8_t c_len_extra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+constexpr float FIXED_DENSITY = 0.2f;  // a fixed-code block: taken as about 1.6 bytes of output per input byte
+
+__device__ float2 header_density(const uint32_t* w, uint64_t end_word, uint64_t bit) {
+    const float2 none = make_float2(0.f, 0.f);
+    LaneBits b;
+    b.init(w, end_word, bit);
+    b.drop(1);
+    const int type = (int)b.get(2);
+    if (type == 0) return make_float2(0.125f, 0.f);  // stored: copied, no codes
+    if (type == 1) return make_float2(FIXED_DENSITY, FIXED_DENSITY / 1.6f);
+    if (type != 2) return none;
+    const int hlit = (int)b.get(5) + 257, hdist = (int)b.get(5) + 1, hclen = (int)b.get(4) + 4;
+    if (hlit > 286 || hdist > 30) return none;
+    uint8_t cl[19] = {};
+    for (int i = 0; i < hclen; i++) cl[c_cl_order[i]] = (uint8_t)b.get(3);
+    uint16_t ccount[16] = {};
+    for (int i = 0; i < 19; i++) ccount[cl[i]]++;
+    ccount[0] = 0;
+    if (kraft_counts(ccount) != 0) return none;
+    uint8_t sorted[19];
+    {
+        uint8_t offs[8];
+        offs[1] = 0;
+        for (int l = 1; l < 7; l++) offs[l + 1] = (uint8_t)(offs[l] + ccount[l]);
+        for (int s = 0; s < 19; s++)
+            if (cl[s]) sorted[offs[cl[s]]++] = (uint8_t)s;
+    }
+    float out = 0.f, bits = 0.f, p_match = 0.f, dist_bits = 0.f, p_dist = 0.f;
+    const int total = hlit + hdist;
+    int prev = 0;
+    for (int i = 0; i < total;) {
+        const uint32_t peek = b.peek(7);
+        int code = 0, first = 0, index = 0, sym = -1;
+        for (int len = 1; len <= 7; len++) {  // canonical decode, one bit at a time
+            code |= (int)((peek >> (len - 1)) & 1);
+            const int c = ccount[len];
+            if (code - c < first) {
+                b.drop(len);
+                sym = sorted[index + (code - first)];
+                break;
+            }
+            index += c;
+            first = (first + c) << 1;
+            code <<= 1;
+        }
+        if (sym < 0) return none;
+        int rep = 1, val = sym;
+        if (sym == 16) {
+            if (i == 0) return none;
+            val = prev;
+            rep = 3 + (int)b.get(2);
+        } else if (sym == 17) {
+            val = 0;
+            rep = 3 + (int)b.get(3);
+        } else if (sym == 18) {
+            val = 0;
+            rep = 11 + (int)b.get(7);
+        }
+        if (i + rep > total) return none;
+        if (val) {
+            const float pr = exp2f(-(float)val);
+            for (int q = i; q < i + rep; q++) {
+                if (q < 256) {
+                    out += pr;
+                    bits += pr * (float)val;
+                } else if (q == 256) {
+                    bits += pr * (float)val;
+                } else if (q < hlit) {
+                    const int s = q - 257 < 28 ? q - 257 : 28;
+                    const int x = c_len_extra[s];
+                    out += pr * ((float)c_len_base[s] + 0.5f * (float)((1 << x) - 1));
+                    bits += pr * (float)(val + x);
+                    p_match += pr;
+                } else {
+                    const int d = q - hlit;
+                    dist_bits += pr * (float)(val + (d < 4 ? 0 : (d - 2) / 2));
+                    p_dist += pr;
+                }
+            }
+        }
+        prev = val;
+        i += rep;
+    }
+    if (p_dist > 0.f) bits += p_match * dist_bits / p_dist;
+    return bits > 0.f ? make_float2(out / bits, 1.f / bits) : none;
+}
+
+__global__ void k_density(const uint32_t* __restrict__ w, uint64_t end_word, const uint64_t* __restrict__ bits, uint64_t n,
+                          float2* __restrict__ out) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = bits[i] == UINT64_MAX ? make_float2(0.f, 0.f) : header_density(w, end_word, bits[i]);
+}
+
 }  // namespace
+
+int launch_density(const uint8_t* d_in, uint64_t end_word, const uint64_t* bits, uint64_t n, float2* out, void* stream) {
+    if (!n) return 0;
+    const uint64_t want = (n + 127) / 128, cap = (uint64_t)sm_count() * 16;
+    k_density<<<(unsigned)(want < cap ? want : cap), 128, 0, (cudaStream_t)stream>>>((const uint32_t*)d_in, end_word, bits, n,
+                                                                                     out);
+    return 1;
+}
 
 int launch_stored_scan(const uint8_t* d_in, uint64_t byte_lo, uint64_t byte_hi, uint64_t end_word, uint64_t end_byte,
                        StoredCand* out, unsigned* n, unsigned cap, void* stream) {
