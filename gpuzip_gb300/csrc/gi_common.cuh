@@ -54,6 +54,9 @@ constexpr uint32_t JOB_CHECK_REFS = 1;
 // the job's output is not kept: it writes over its first extent again and again (which must hold
 // DISCARD_EXTENT symbols: a stored block and a match), for decodes only their results are wanted from
 constexpr uint32_t JOB_DISCARD = 2;
+// a job whose start is known to be in step (a segment's or a stream's start): never given up
+constexpr uint32_t JOB_TRUSTED = 4;
+constexpr int32_t GIVE_UP_AFTER = 2;  // DecodeArgs.give_up of the decode paths (0 in the rescue)
 constexpr uint32_t DISCARD_EXTENT = 65536 + 512;
 
 struct JobResult {
@@ -71,6 +74,7 @@ struct JobResult {
     uint64_t symbols;    // literals and matches decoded (an encoder's blocks hold a regular number)
     uint64_t last_block_bit;  // header of the last block it began (UINT64_MAX: none)
     uint64_t last_block_out;  // symbols written before that header
+    uint64_t t_begin, t_end;  // the GPU's global timer (ns) when the job began and ended (diagnostics)
 };
 
 // a run of a job's output in the pool; job k's first extent is extent k
@@ -109,7 +113,13 @@ struct DecodeArgs {
     int32_t njobs;
     int32_t ext_cap;
     int32_t stored_cap;
-    int32_t pad;
+    // a job that starts inside a block (at a probe point), is not JOB_TRUSTED, and passes this
+    // many targets at block starts (AT_BLOCK) without landing on one stops there (S_STOPPED, its
+    // exact state in resume): a decoder in step lands on every real block start it reaches, so it
+    // is out of step, decoding garbage that a periodic code stream can keep valid for hundreds of
+    // kilobytes. (Jobs from block starts never give up: the finder's spurious hits inside a block
+    // of near-random codes would stop correct ones.) 0: never.
+    int32_t give_up;
     uint16_t* pool;
     uint64_t pool_cap;
     JobResult* res;

@@ -54,6 +54,8 @@ struct Job1 {
     const Start* tg;
     int t, tend;        // next target, end of the stream's targets
     uint64_t tbit;      // targets[t].bit, or UINT64_MAX
+    int passed;         // block-start targets passed without landing (DecodeArgs.give_up)
+    int give_up;        // 0: never
 };
 
 // per-warp shared memory: the decoder's tables, and the state of its current job that the hot loop
@@ -198,6 +200,12 @@ struct Ctx {
     Tables* T;
     int lane;
 };
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Bit reader, identical in every lane
 struct Bits {
@@ -485,9 +493,13 @@ __device__ void decode_job(Ctx& C, int k) {
     j.t = J.tfirst;
     j.tend = S.target_end;
     j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
+    j.passed = 0;
+    j.give_up = (J.flags & JOB_TRUSTED) || J.start.mode == AT_BLOCK ? 0 : C.a.give_up;
     const bool check_refs = (J.flags & JOB_CHECK_REFS) != 0;
 
     JobResult& r = T.r;
+    r.t_begin = global_ns();
+    r.t_end = r.t_begin;
     r.eob_bit = UINT64_MAX;
     r.eob_out = 0;
     r.status = S_OK;
@@ -544,6 +556,7 @@ __device__ void decode_job(Ctx& C, int k) {
         if (!in_block) {
             uint64_t p = br.pos();
             while (j.tbit < p) {
+                j.passed += j.tg[j.t].mode == AT_BLOCK;
                 j.t++;
                 j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
             }
@@ -551,7 +564,7 @@ __device__ void decode_job(Ctx& C, int k) {
                 r.landed = j.t;
                 break;
             }
-            if (p >= j.stop) {
+            if (p >= j.stop || (j.give_up && j.passed >= j.give_up)) {
                 r.status = S_STOPPED;
                 r.resume = Start{p, p, AT_BLOCK, -1, {0, 0, 0, 0, 0, 0}};
                 break;
@@ -661,6 +674,7 @@ __device__ void decode_job(Ctx& C, int k) {
                 // a target at or before this symbol boundary: land on it when it is a boundary
                 // of this block (same tables), else pass it
                 while (j.tbit < p) {
+                    j.passed += j.tg[j.t].mode == AT_BLOCK;
                     j.t++;
                     j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
                 }
@@ -670,8 +684,14 @@ __device__ void decode_job(Ctx& C, int k) {
                         r.landed = j.t;
                         break;
                     }
+                    j.passed += tt.mode == AT_BLOCK;
                     j.t++;
                     j.tbit = j.t < j.tend ? j.tg[j.t].bit : UINT64_MAX;
+                }
+                if (j.give_up && j.passed >= j.give_up) {  // out of step: stop where it is
+                    r.status = S_STOPPED;
+                    r.resume = Start{p, header, mode, (int8_t)r.end_final, {0, 0, 0, 0, 0, 0}};
+                    break;
                 }
                 lim2 = j.tbit < j.limit ? j.tbit : j.limit;
                 continue;
@@ -724,6 +744,7 @@ __device__ void decode_job(Ctx& C, int k) {
     r.end_bit = br.pos();
     r.out_len = o.done + o.op;
     r.cycles = (uint64_t)(clock64() - t_begin);
+    r.t_end = global_ns();
     if (lane == 0) {
         C.a.ext[o.ext].len = o.op;
         C.a.res[k] = r;

@@ -386,28 +386,34 @@ static int kraft(const uint8_t* lens, int n, int* nonzero, int* ones) {
     return left > 0 ? 1 : 0;
 }
 
-/* does bit look like the start of a dynamic block (inflate.cuh:315-332) */
-int oracle_plausible_dynamic_header(const uint8_t* in, uint64_t size, uint64_t bit) {
-    uint8_t* pad = (uint8_t*)calloc((size_t)size + 16, 1);
-    if (!pad) return 0;
-    memcpy(pad, in, (size_t)size);
+/* does bit look like the start of a dynamic block (inflate.cuh:315-332); pad: the input followed
+ * by at least 16 zero bytes */
+static int plausible_padded(const uint8_t* pad, uint64_t size, uint64_t bit) {
     obits b = {pad, size, size * 8, bit};
     uint32_t h = peek(&b, 17);
     int ok = 0;
     if (((h >> 1) & 3) == 2 && ((h >> 3) & 31) <= 29 && ((h >> 8) & 31) <= 29) {
         b.pos += 3;
-        ohuff* clh = (ohuff*)malloc(sizeof(ohuff));
+        ohuff clh_store;
+        ohuff* clh = &clh_store;
         uint8_t lens[320];
         int hlit, hdist, nz, ones;
-        if (clh && read_code_lengths(&b, clh, lens, &hlit, &hdist) == 0) {
+        if (read_code_lengths(&b, clh, lens, &hlit, &hdist) == 0) {
             int r = kraft(lens, hlit, &nz, &ones);
             if (!(r < 0 || (r > 0 && !(nz == 1 && ones == 1)))) {
                 r = kraft(lens + hlit, hdist, &nz, &ones);
                 if (!(r < 0 || (r > 0 && !(nz == 0 || (nz == 1 && ones == 1))))) ok = b.pos <= b.size_bits;
             }
         }
-        free(clh);
     }
+    return ok;
+}
+
+int oracle_plausible_dynamic_header(const uint8_t* in, uint64_t size, uint64_t bit) {
+    uint8_t* pad = (uint8_t*)calloc((size_t)size + 16, 1);
+    if (!pad) return 0;
+    memcpy(pad, in, (size_t)size);
+    const int ok = plausible_padded(pad, size, bit);
     free(pad);
     return ok;
 }

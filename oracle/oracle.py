@@ -59,6 +59,9 @@ def lib():
         _lib.oracle_plausible_dynamic_header.restype = ctypes.c_int
         _lib.oracle_first_headers.argtypes = [u8p, u64, u64, u64, u64, ctypes.c_void_p, u64]
         _lib.oracle_first_headers.restype = None
+        _lib.oracle_inflate_parallel.argtypes = [u8p, u64, u64, u64, ctypes.c_void_p, u64, u64p, ctypes.c_int,
+                                                 ctypes.POINTER(ctypes.c_double)]
+        _lib.oracle_inflate_parallel.restype = ctypes.c_int
     return _lib
 
 
@@ -105,6 +108,18 @@ def ref_inflate(data, max_out=None):
     if max_out is None:
         max_out = max(64 << 20, len(data) * 16)
     return _run(r.ref_inflate, data, max_out)
+
+
+def inflate_parallel(data, out_cap, threads, scan_bytes=None, chunk_bytes=4096):
+    """(status, output bytes, phase seconds) of the multi-threaded CPU inflate (the reference's
+    speculative CPU decoder restated): the first up to out_cap bytes of output, one block start
+    searched per chunk_bytes of the first scan_bytes of input (all of it by default)."""
+    out = ctypes.create_string_buffer(max(1, out_cap))
+    n = ctypes.c_uint64(0)
+    secs = (ctypes.c_double * 3)()
+    rc = lib().oracle_inflate_parallel(bytes(data), len(data), len(data) if scan_bytes is None else scan_bytes, chunk_bytes,
+                                       out, out_cap, ctypes.byref(n), threads, secs)
+    return rc, (out.raw[:n.value] if rc == OK else b""), list(secs)
 
 
 def crc32(data, crc=0):

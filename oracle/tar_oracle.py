@@ -15,6 +15,17 @@ UNKNOWN, EXACT, SUSPECT, INFERRED = 0, 1, 2, 3
 MAX_META = 64 << 20  # src/rescue.rs:415
 
 
+def rust_usize(b):
+    """bytes b read as Rust's str::parse::<usize> (or ::<u64>) reads them: one optional '+', then
+    one or more ASCII digits, below 2**64; None otherwise (Python's int() would also take spaces,
+    underscores and a '-')."""
+    s = b[1:] if b[:1] == b"+" else b
+    if not s or any(c < 0x30 or c > 0x39 for c in s):
+        return None
+    v = int(s)
+    return v if v < 1 << 64 else None
+
+
 def octal(field):
     """A tar number field (src/rescue.rs:374-384): GNU base-256, or octal digits up to NUL or
     space; None when the digits do not parse."""
@@ -101,11 +112,8 @@ def untar(data, mask, crc_check=-1, damaged=0, hidden_damage=0):
                     sp = rec.find(b" ")
                     if sp < 0:
                         break
-                    try:
-                        n = int(rec[:sp].decode("utf-8", "replace"))
-                    except ValueError:
-                        break
-                    if n <= 0 or p + n > len(buf):
+                    n = rust_usize(bytes(rec[:sp]))
+                    if n is None or n <= 0 or p + n > len(buf):
                         break
                     kv = buf[p + sp + 1:p + n - 1]
                     eq = kv.find(b"=")
@@ -116,10 +124,7 @@ def untar(data, mask, crc_check=-1, damaged=0, hidden_damage=0):
                         elif k == b"linkpath":
                             pax_link = v
                         elif k == b"size":
-                            try:
-                                pax_size = int(v)
-                            except ValueError:
-                                pax_size = None
+                            pax_size = rust_usize(v.encode("utf-8", "surrogateescape"))
                     p += n
 
     while True:

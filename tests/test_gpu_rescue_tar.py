@@ -45,3 +45,20 @@ def test_full_size_tar_rescue_matches_reference():
         del r
         for k in ("rc", "out_len", "data_sha256", "mask_sha256", "mask_counts", "stats", "pieces_sha256"):
             assert got[k] == gi[k], "infer " + k
+
+
+def test_tar_walk_reads_a_plus_signed_pax_length():
+    """The GPU tar walk reads a pax record's length as the reader does (Rust's parse::<usize>,
+    which takes one leading '+'): the file is named by the record's path."""
+    import zlib
+
+    sys.path.insert(0, HERE)
+    from gpuzip_gb300 import workloads as W
+    from test_tar_oracle import plus_pax_tar
+
+    name = "deep/" + "p" * 120 + "/file.txt"
+    tar, _ = plus_pax_tar(name)
+    member = W.gzip_wrap(W.raw_deflate(tar, 6), zlib.crc32(tar), len(tar))
+    r = gzrescue.rescue_tar(member)
+    assert r["rc"] == 0 and r["tar"]["intact"] == 1
+    assert [f[0] for f in r["tar"]["files"]] == [name]

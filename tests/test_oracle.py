@@ -93,3 +93,23 @@ def test_first_headers_are_real_block_starts():
         for f in first:
             if f != 2**64 - 1:
                 assert r.ref_plausible_dynamic_header(s, len(s), f) == 1
+
+
+def test_parallel_cpu_inflate_matches_zlib():
+    """The multi-threaded CPU baseline (the reference's speculative CPU decoder restated) gives
+    zlib's bytes for every block kind, for a mixed member with several chunk sizes and thread
+    counts, and for a prefix of it."""
+    import zlib
+
+    for name, s in W.fuzz_streams().items():
+        want = zlib.decompressobj(-15).decompress(s)
+        rc, out, _ = oracle.inflate_parallel(s, len(want) + 16, 4)
+        assert rc == oracle.OK and out == want, name
+    member, info = W.mixed_member(seed=2, nseg=24, want_raw=True)
+    body = member[10:10 + info["deflate_size"]]
+    for threads, chunk in ((1, 4096), (3, 16 << 10), (8, 256 << 10)):
+        rc, out, secs = oracle.inflate_parallel(body, info["size"], threads, chunk_bytes=chunk)
+        assert rc == oracle.OK and out == info["raw"], (threads, chunk)
+        assert len(secs) == 3
+    rc, out, _ = oracle.inflate_parallel(body, 5 << 20, 4, scan_bytes=len(body) // 2)
+    assert rc == oracle.OK and out == info["raw"][:5 << 20]

@@ -68,3 +68,33 @@ def test_header_checksum_forms():
     # digits stop at a NUL or a space (none: 0); what is left is trimmed and must be octal
     assert T.octal(b"   ") == 0 and T.octal(b"\0\0") == 0 and T.octal(b"0000644\0") == 0o644
     assert T.octal(b"\t\t") is None and T.octal(b"8") is None and T.octal(b"+17") == 0o17
+
+
+def plus_pax_tar(name, length_prefix="+"):
+    """A tar whose one file gets its path from a pax record written with a leading '+' on its
+    length ("+NN path=...\\n"), which Rust's parse::<usize> accepts."""
+    rec = b" path=" + name.encode() + b"\n"
+    n = len(rec) + 2
+    while len(length_prefix + str(n)) + len(rec) != n:
+        n = len(length_prefix + str(n)) + len(rec)
+    pax = (length_prefix + str(n)).encode() + rec
+    data = b"the file's bytes\n" * 40
+    parts = [W.ustar_header("PaxHeaders/plus", len(pax), typeflag=b"x"), pax, bytes(-len(pax) % 512),
+             W.ustar_header(name[-90:], len(data)), data, bytes(-len(data) % 512), bytes(1024)]
+    return b"".join(parts), len(pax) + 512 * 2  # (tar, an offset inside the file's data)
+
+
+def test_pax_record_length_with_a_plus_sign():
+    name = "deep/" + "p" * 120 + "/file.txt"
+    tar, inside = plus_pax_tar(name)
+    mask = bytearray([T.EXACT]) * len(tar)
+    mask[inside + 600] = T.SUSPECT  # the file is listed by name among the suspect ones
+    assert T.untar(tar, bytes(mask))["suspect"] == [name]
+    assert T.rust_usize(b"+17") == 17 and T.rust_usize(b"17") == 17
+    for bad in (b"", b"+", b"-3", b" 3", b"1_0", b"3 ", b"++3", str(1 << 64).encode()):
+        assert T.rust_usize(bad) is None, bad
+    # a length Rust does not parse ends the records: the header's own (shortened) name is used
+    tar_bad, inside = plus_pax_tar(name, length_prefix="0x")
+    mask = bytearray([T.EXACT]) * len(tar_bad)
+    mask[inside + 600] = T.SUSPECT
+    assert T.untar(tar_bad, bytes(mask))["suspect"] == [name[-90:]]
