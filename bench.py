@@ -477,7 +477,8 @@ def run_serve(args, ws, rank, local):
         return {"p50": pct(lat, 0.50), "p99": pct(lat, 0.99), "p999": pct(lat, 0.999), "max": round(max(lat) * 1e3, 3)}
 
     def served(saturate):
-        srv = gpuinflate.Server(local, workers=args.workers, hbm_budget=args.hbm_budget)
+        srv = gpuinflate.Server(local, workers=args.workers, hbm_budget=args.hbm_budget,
+                                rescue_workers=args.rescue_workers)
         for k in range(min(8, n)):  # warm-up: first launches, first touch of the output buffers
             srv.submit((req_ptr[k], req_size[k]), flags=req_flags[k], tag=1 << 40 | k)
         srv.drain()
@@ -863,6 +864,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--pool", type=int, default=256, help="serve: distinct members requests draw from")
     ap.add_argument("--workers", type=int, default=3, help="serve: concurrent decode loops")
+    ap.add_argument("--rescue-workers", type=int, default=3, help="serve: concurrent rescue loops (at most 4)")
     ap.add_argument("--hbm-budget", type=float, default=120e9)
     ap.add_argument("--bgzf-mb", type=int, default=256, help="bgzf: MiB of output")
     args = ap.parse_args()
@@ -1002,6 +1004,7 @@ def main():
             "gpu_launches": gpu_launches,
             "stages_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()},
             "jobs_per_step": profs[0]["jobs"], "segments_per_step": st.segments,
+            "tuning": {k: profs[-1][k] for k in ("probe_spacing_bits", "probe_lead_bits", "job_share_div", "tuned")},
         }
         print(json.dumps(line), flush=True)
     g.close()

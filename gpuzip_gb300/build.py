@@ -11,7 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libgpuinflate.so")
-SOURCES = ["gi_find.cu", "gi_decode.cu", "gi_resolve.cu", "gi_engine.cu", "gi_noalloc.cu", "gi_server.cu", "gi_rescue.cu"]
+SOURCES = ["gi_find.cu", "gi_decode.cu", "gi_resolve.cu", "gi_engine.cu", "gi_noalloc.cu", "gi_server.cu", "gi_rescue.cu",
+           "gi_tarindex.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

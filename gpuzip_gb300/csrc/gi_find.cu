@@ -233,6 +233,9 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
                     uint64_t m = ~(lo64 >> 1) & (lo64 >> 2);                          // BTYPE = 2
                     m &= ~((lo64 >> 4) & (lo64 >> 5) & (lo64 >> 6) & (lo64 >> 7));    // HLIT <= 29
                     m &= ~((lo64 >> 9) & (lo64 >> 10) & (lo64 >> 11) & (lo64 >> 12)); // HDIST <= 29
+                    // BFINAL = 0 for the decode paths: only a stream's last block is final, and the
+                    // decoder before it reaches it in step (the rescue keeps every header)
+                    if (!ALL) m &= ~lo64;
                     mask = (uint32_t)m;
                     uint64_t base = wi * 32;
                     if (base < lo) mask &= ~0u << (uint32_t)(lo - base);

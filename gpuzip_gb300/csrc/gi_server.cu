@@ -98,8 +98,11 @@ struct gi_server {
     bool stop = false;
     gi_server_stats st{};
     std::mutex done_m;  // callbacks never run two at once
-    std::thread admitter, rescuer;
-    std::vector<std::thread> workers;
+    std::thread admitter;
+    std::vector<std::thread> workers, rescuers;
+    // the rescues' device memory: an allowance carved from the budget, used by estimate
+    uint64_t rescue_budget = 0, rescue_used = 0;
+    uint32_t rescues_running = 0;
 
     double now() const { return std::chrono::duration<double>(clk::now() - t0).count(); }
 };
@@ -303,20 +306,33 @@ int rescue_status(int gr) {
     }
 }
 
-// the rescue requests, in arrival order (the GPU work of a rescue runs beside the passes)
+// A rescue's device peak, estimated: about 24 bytes per output byte (the input, the links'
+// symbols, the pass's entries, bytes, certainty, output and mask) for its output guess.
+uint64_t rescue_need(const Request* r) { return 24 * std::max<uint64_t>(r->out_guess, r->size) + 2 * r->size; }
+
+// The rescue requests, in arrival order, on rescue_workers loops (their GPU work runs beside the
+// passes, each on its own stream): the next one starts when its estimated device peak fits what
+// the rescues in progress leave of the allowance (or when none is in progress).
 void rescue_loop(gi_server* s) {
     cudaSetDevice(s->cfg.device);
     std::unique_lock<std::mutex> l(s->m);
     for (;;) {
-        s->cv.wait(l, [&] { return s->stop || !s->rescue.empty(); });
+        s->cv.wait(l, [&] {
+            return s->stop || (!s->rescue.empty() && (s->rescues_running == 0 ||
+                                                       s->rescue_used + rescue_need(s->rescue.front()) <= s->rescue_budget));
+        });
         if (s->rescue.empty()) return;
         Request* r = s->rescue.front();
         s->rescue.pop_front();
+        const uint64_t need = rescue_need(r);
+        s->rescue_used += need;
+        s->rescues_running++;
         r->t_admit = r->t_start = s->now();
+        const uint64_t keep = s->rescue_budget / (4 * std::max<uint32_t>(1, s->cfg.rescue_workers));
         l.unlock();
         std::vector<uint8_t> buf;
         uint64_t out_size = 0;
-        int rc = gz::rescue_for_server(s->cfg.device, r->in, r->size, buf, out_size);
+        int rc = gz::rescue_for_server(s->cfg.device, r->in, r->size, buf, out_size, keep);
         gi_result res{r->tag, rescue_status(rc), 0, rc == 0 ? out_size : 0, r->size, r->t_submit, r->t_admit,
                       r->t_start, 0, 1, s->cfg.workers};
         {
@@ -325,6 +341,8 @@ void rescue_loop(gi_server* s) {
             s->done(s->user, &res, res.status == GI_OK ? buf.data() : nullptr);
         }
         l.lock();
+        s->rescue_used -= need;
+        s->rescues_running--;
         s->st.completed++;
         s->st.failed += res.status != GI_OK;
         s->st.out_bytes += res.out_size;
@@ -341,7 +359,8 @@ void teardown(gi_server* s) {
         s->cv.notify_all();
     }
     if (s->admitter.joinable()) s->admitter.join();
-    if (s->rescuer.joinable()) s->rescuer.join();
+    for (auto& t : s->rescuers)
+        if (t.joinable()) t.join();
     for (auto& t : s->workers)
         if (t.joinable()) t.join();
     cudaSetDevice(s->cfg.device);
@@ -375,13 +394,17 @@ GI_API int gi_server_create(const gi_server_config* cfg, gi_done done, void* use
     if (!c.max_batch) c.max_batch = 4096;
     c.max_batch = std::min(c.max_batch, MAX_BATCH);
     if (!c.hbm_budget) c.hbm_budget = DEFAULT_BUDGET;
+    if (!c.rescue_workers) c.rescue_workers = 3;
+    if (c.rescue_workers > 4) return fail(GI_ERR_ARG, "too many rescue workers (at most 4)");
+    const uint64_t rescue_budget = std::clamp<uint64_t>(c.hbm_budget / 6, 4ull << 30, 24ull << 30);
+    if (rescue_budget >= c.hbm_budget) return fail(GI_ERR_ARG, "HBM budget too small for the rescues' allowance");
     if (cudaSetDevice(c.device) != cudaSuccess || cudaFree(nullptr) != cudaSuccess) {
         cudaGetLastError();
         return fail(GI_ERR_GPU, "no usable GPU");
     }
     uint32_t pass_mb = c.pass_out_mb;
     if (!pass_mb) {
-        double fit = 0.6 * (double)c.hbm_budget / (c.workers * CTX_BYTES_PER_PASS_BYTE) / (1 << 20);
+        double fit = 0.6 * (double)(c.hbm_budget - rescue_budget) / (c.workers * CTX_BYTES_PER_PASS_BYTE) / (1 << 20);
         pass_mb = (uint32_t)std::min<double>(DEFAULT_PASS_MB, fit);
     }
     if (pass_mb < MIN_PASS_MB) return fail(GI_ERR_ARG, "HBM budget too small for the workers' pass buffers");
@@ -407,8 +430,9 @@ GI_API int gi_server_create(const gi_server_config* cfg, gi_done done, void* use
     cudaMemGetInfo(&free1, &total);
     const uint64_t ctx_bytes = free0 > free1 ? free0 - free1 : 0;
     uint64_t arena = c.arena_bytes;
-    if (!arena) arena = c.hbm_budget > ctx_bytes ? std::min(c.hbm_budget - ctx_bytes, ARENA_MAX) : 0;
-    if (arena < ARENA_MIN || ctx_bytes + arena > c.hbm_budget) {
+    const uint64_t room = c.hbm_budget - rescue_budget;  // the passes' buffers and the arena
+    if (!arena) arena = room > ctx_bytes ? std::min(room - ctx_bytes, ARENA_MAX) : 0;
+    if (arena < ARENA_MIN || ctx_bytes + arena > room) {
         teardown(s);
         return fail(GI_ERR_ARG, "HBM budget too small: the pass buffers take " + std::to_string(ctx_bytes >> 20) +
                                     " MiB and the arena needs at least 64 MiB");
@@ -432,8 +456,9 @@ GI_API int gi_server_create(const gi_server_config* cfg, gi_done done, void* use
     s->st.workers = c.workers;
     s->st.device_bytes = ctx_bytes + arena;
     s->st.arena_bytes = arena;
+    s->rescue_budget = rescue_budget;
     s->admitter = std::thread(admit_loop, s);
-    s->rescuer = std::thread(rescue_loop, s);
+    for (uint32_t w = 0; w < c.rescue_workers; w++) s->rescuers.emplace_back(rescue_loop, s);
     for (uint32_t w = 0; w < c.workers; w++) s->workers.emplace_back(work_loop, s, (int)w);
     *out = s;
     return GI_OK;

@@ -39,6 +39,10 @@ EXPORTED = (
     "gi_server_clock",
     "gi_server_read_stats",
     "gi_server_destroy",
+    "gi_tar_index_device",
+    "gi_tar_entries",
+    "gi_tar_end",
+    "gi_tar_free",
 )
 
 GI_STREAM_GZIP = 1
@@ -73,7 +77,9 @@ class Profile(ctypes.Structure):
     _fields_ = [("size", ctypes.c_uint32), ("launches", ctypes.c_uint32), ("kernel_ms", ctypes.c_double * 7),
                 ("decode_launches", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("in_bytes", ctypes.c_uint64),
                 ("out_bytes", ctypes.c_uint64), ("jobs", ctypes.c_uint64), ("extents", ctypes.c_uint64),
-                ("stored_blocks", ctypes.c_uint64), ("probes", ctypes.c_uint64)]
+                ("stored_blocks", ctypes.c_uint64), ("probes", ctypes.c_uint64),
+                ("probe_spacing_bits", ctypes.c_uint32), ("probe_lead_bits", ctypes.c_uint32),
+                ("job_share_div", ctypes.c_float), ("tuned", ctypes.c_uint32)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("size", "kernel_ms")}
@@ -114,11 +120,18 @@ ENTRY_SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ZipE
                               ctypes.c_void_p, ctypes.c_size_t)
 
 
+class TarEntry(ctypes.Structure):
+    """gi_tar_entry (gpuinflate.h): one entry of a tar archive in device memory"""
+
+    _fields_ = [("name", ctypes.c_char_p), ("header", ctypes.c_uint64), ("offset", ctypes.c_uint64),
+                ("size", ctypes.c_uint64), ("type", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 class ServerConfig(ctypes.Structure):
     """gi_server_config (gpuinflate.h)"""
 
     _fields_ = [("size", ctypes.c_uint32), ("device", ctypes.c_int32), ("workers", ctypes.c_uint32),
-                ("max_batch", ctypes.c_uint32), ("pass_out_mb", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("max_batch", ctypes.c_uint32), ("pass_out_mb", ctypes.c_uint32), ("rescue_workers", ctypes.c_uint32),
                 ("hbm_budget", ctypes.c_uint64), ("arena_bytes", ctypes.c_uint64)]
 
 
@@ -215,6 +228,14 @@ def load(path=None):
     lib.gi_server_read_stats.restype = ctypes.c_int
     lib.gi_server_destroy.argtypes = [vp]
     lib.gi_server_destroy.restype = None
+    lib.gi_tar_index_device.argtypes = [vp, vp, u64, ctypes.POINTER(vp)]
+    lib.gi_tar_index_device.restype = ctypes.c_int
+    lib.gi_tar_entries.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(TarEntry))]
+    lib.gi_tar_entries.restype = ctypes.c_uint32
+    lib.gi_tar_end.argtypes = [vp]
+    lib.gi_tar_end.restype = u64
+    lib.gi_tar_free.argtypes = [vp]
+    lib.gi_tar_free.restype = None
     _lib = lib
     return lib
 
@@ -425,6 +446,22 @@ class Gpu:
             raise InflateError(rc, "profile")
         return p
 
+    def tar_index_device(self, d_tar, size):
+        """gi_tar_index_device: the entries of the tar archive at device pointer d_tar (size
+        bytes), as dicts (name, header, offset, size, type), and the bytes the archive took."""
+        t = ctypes.c_void_p()
+        rc = self.lib.gi_tar_index_device(self.ctx, ctypes.c_void_p(d_tar), size, ctypes.byref(t))
+        if rc != GI_OK:
+            raise InflateError(rc, self.lib.gi_last_error(self.ctx).decode(errors="replace"))
+        try:
+            ep = ctypes.POINTER(TarEntry)()
+            n = self.lib.gi_tar_entries(t, ctypes.byref(ep))
+            out = [{"name": ep[i].name.decode("utf-8", "surrogateescape"), "header": ep[i].header,
+                    "offset": ep[i].offset, "size": ep[i].size, "type": ep[i].type} for i in range(n)]
+            return out, self.lib.gi_tar_end(t)
+        finally:
+            self.lib.gi_tar_free(t)
+
     def last_crc32(self):
         return self.lib.gi_last_crc32(self.ctx)
 
@@ -452,7 +489,7 @@ class Server:
     with the output valid only during that call."""
 
     def __init__(self, device=0, workers=0, max_batch=0, pass_out_mb=0, hbm_budget=0, arena_bytes=0,
-                 keep_output=False, on_done=None, path=None):
+                 keep_output=False, on_done=None, path=None, rescue_workers=0):
         self.lib = load(path)
         self.results = {}
         self._inputs = {}
@@ -479,8 +516,8 @@ class Server:
                 self.results[r.tag] = d
 
         self._cb = DONE(_cb)
-        cfg = ServerConfig(ctypes.sizeof(ServerConfig), device, workers, max_batch, pass_out_mb, 0, int(hbm_budget),
-                           int(arena_bytes))
+        cfg = ServerConfig(ctypes.sizeof(ServerConfig), device, workers, max_batch, pass_out_mb, rescue_workers,
+                           int(hbm_budget), int(arena_bytes))
         srv = ctypes.c_void_p()
         err = ctypes.create_string_buffer(512)
         rc = self.lib.gi_server_create(ctypes.byref(cfg), self._cb, None, ctypes.byref(srv), err, 512)

@@ -157,6 +157,14 @@ typedef struct {
     uint64_t out_bytes;     /* bytes produced */
     uint64_t jobs, extents, stored_blocks;
     uint64_t probes;        /* probe points (resynchronization inside long blocks) */
+    /* the planner's setting the call used, chosen by the context's autotuner for this class of
+     * stream (gi_inflate, gi_inflate_device, gi_inflate_gzip): the farthest apart probe points
+     * are (bits), the bits a probe decodes before its point, the divisor of a decoder's average
+     * work that gives one job's share; tuned: 0 while the class's candidates are being tried
+     * (one per call), 1 once the fastest was chosen */
+    uint32_t probe_spacing_bits, probe_lead_bits;
+    float job_share_div;
+    uint32_t tuned;
 } gi_profile;
 
 GI_API int gi_last_profile(const gi_ctx* ctx, gi_profile* profile);
@@ -174,6 +182,31 @@ GI_API int gi_last_profile(const gi_ctx* ctx, gi_profile* profile);
  * is computed on the host by its caller). */
 GI_API int gi_crc32_device_noalloc(int device, const void* d_data, uint64_t size, uint32_t* d_crc, void* stream,
                                    char* err, size_t err_len);
+
+/* The entries of a tar archive that lies decoded in GPU memory (by gi_inflate_device, say, from a
+ * .tar.gz member): every 512-byte block is tested for a header on the GPU at once, then the
+ * chain of headers is walked from the archive's start, GNU long names ('L') and pax records
+ * ('x': path, size) applied to the entry that follows them, up to the all-zero block that ends
+ * the archive. d_tar must be 16-byte aligned. *tar gets the entries in archive order (free with
+ * gi_tar_free); GI_ERR_DATA when a header fails its checksum or the archive ends inside one
+ * (gi_last_error says where). No counterpart in the reference, whose host reads the decoded
+ * stream through a tar reader (src/gz.rs:622-785). */
+typedef struct {
+    const char* name;   /* the entry's path: its pax path, else its GNU long name, else its header's
+                           (a ustar prefix joined to it); valid until gi_tar_free */
+    uint64_t header;    /* offset of its header in the archive */
+    uint64_t offset;    /* offset of its data */
+    uint64_t size;      /* bytes of data */
+    uint32_t type;      /* its typeflag byte: '0' or 0 a file, '5' a folder, '1'/'2' links, ... */
+    uint32_t reserved;
+} gi_tar_entry;
+
+typedef struct gi_tar gi_tar;
+
+GI_API int gi_tar_index_device(gi_ctx* ctx, const void* d_tar, uint64_t size, gi_tar** tar);
+GI_API uint32_t gi_tar_entries(const gi_tar* tar, const gi_tar_entry** entries);
+GI_API uint64_t gi_tar_end(const gi_tar* tar);  /* bytes the archive took, through its end block */
+GI_API void gi_tar_free(gi_tar* tar);
 
 /* Every gzip member of a file (a .gz, .tgz, a BGZF file, any concatenation of members), decoded
  * as gpuzip's gz::decode does (src/gz.rs:154-264): header rules of parse_header (FHCRC checked,
@@ -253,8 +286,9 @@ typedef struct {
     uint32_t workers;       /* decode loops, i.e. passes that may run at once (0 = 3) */
     uint32_t max_batch;     /* most requests in one pass (0 = 4096) */
     uint32_t pass_out_mb;   /* output of one pass, MiB (0 = 2048, less when the budget is small) */
-    uint32_t reserved;
-    uint64_t hbm_budget;    /* device bytes the server may hold: pass buffers + arena (0 = 120 GB) */
+    uint32_t rescue_workers; /* rescue loops: GI_REQ_RESCUE requests recovered at once (0 = 3, at most 4) */
+    uint64_t hbm_budget;    /* device bytes the server may hold: pass buffers + arena + the rescues'
+                               allowance (a sixth of the budget, 4-24 GiB; 0 = 120 GB) */
     uint64_t arena_bytes;   /* of which the input arena (0 = the rest of the budget, at most 64 GiB) */
 } gi_server_config;
 

@@ -9,8 +9,9 @@
  * decoded on the GPU at once (one decode from each header, landing on the next), the decisions
  * of a pass are made on the host from those results, and the bytes, their certainty, the CRC-32
  * checks, the one-flipped-bit trials and the scoring of lost window bytes are computed on the GPU.
- * The calls take no context: the library keeps one device (GPUZIP_RESCUE_DEVICE, default 0) and
- * serializes the calls of a process.
+ * The calls take no context: the library keeps one device (GPUZIP_RESCUE_DEVICE, default 0); up to
+ * four calls of a process run at once (each on a rescue slot of its own: its stream, the device
+ * blocks it keeps for its next call, its host tables), further calls wait for a free slot.
  *
  * Not done here (the call behaves as with the option that turns it off): the search for the CRs
  * a Windows-to-Unix transfer removed from a raw stream with its own CRC (cr_restored is 0). */

@@ -117,3 +117,8 @@ def test_members_info_layout():
 def test_zip_entry_layout():
     assert ctypes.sizeof(gpuinflate.ZipEntry) == 40
     assert gpuinflate.ZipEntry.out_size.offset == 16
+
+
+def test_tar_entry_layout():
+    assert ctypes.sizeof(gpuinflate.TarEntry) == 40
+    assert gpuinflate.TarEntry.size.offset == 24 and gpuinflate.TarEntry.type.offset == 32

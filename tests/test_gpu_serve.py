@@ -152,3 +152,28 @@ def test_rescue_requests_beside_passes(mix):
     assert r["out_size"] == alone["stats"]["output_size"] and r["crc32"] == 0
     r = srv.results[101]
     assert r["output"] == expected(good[0]) and r["mask"] == bytes([gzrescue.GR_EXACT]) * len(r["output"])
+
+
+def test_rescues_run_together(mix):
+    """Several rescue requests at once: the server's rescue loops (three) and gr_rescue calls from
+    several host threads run them together, on the rescue slots, and each comes back exactly as
+    when it ran alone."""
+    import concurrent.futures
+
+    from gpuzip_gb300 import gzrescue
+
+    members = [x for x in mix if x["gzip"] and x["size"] > 128 << 10][:6]
+    damaged = [W.zero_sector(x["data"], 11, i) for i, x in enumerate(members)]
+    alone = [gzrescue.rescue(d) for d in damaged]
+    srv = gpuinflate.Server(0, workers=2, hbm_budget=60e9, keep_output=True, rescue_workers=3)
+    for i, d in enumerate(damaged):
+        srv.submit(d, flags=GZIP | gpuinflate.GI_REQ_RESCUE, tag=i)
+    srv.drain()
+    srv.close()
+    for i, a in enumerate(alone):
+        r = srv.results[i]
+        assert r["status"] == 0 and r["output"] == a["data"] and r["mask"] == a["mask"], i
+    with concurrent.futures.ThreadPoolExecutor(4) as ex:
+        together = list(ex.map(gzrescue.rescue, damaged))
+    for a, t in zip(alone, together):
+        assert t["data"] == a["data"] and t["mask"] == a["mask"] and t["stats"] == a["stats"]
