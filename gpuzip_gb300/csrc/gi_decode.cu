@@ -428,7 +428,9 @@ __device__ bool new_extent(Ctx& C, Out& o, uint64_t need, const Start& state, in
 // end-of-block code, -1 invalid data with no code at all, -2 invalid data after a length symbol
 // was read (a length or distance symbol that does not exist, or - check_refs - a match reaching
 // before the stream's start). The reference counts a symbol at its length code, before the rest
-// is checked (inflate.cuh:449-457), so a -2 is one more symbol read.
+// is checked (inflate.cuh:449-457), so a -2 is one more symbol read. As there, a code that is in
+// the table but names no length (286, 287) or no distance (30, 31) is read before it is refused,
+// and a bit pattern that is no code at all is not: where the decode ends on an error is the same.
 __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int lane, bool check_refs) {
     br.need(32);
     uint32_t e = T.lit[(uint32_t)br.buf & ((1u << LB) - 1)];
@@ -457,7 +459,12 @@ __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int
         br.cnt -= n;
         return 1;
     }
-    if (kind == K_BAD) return -2;
+    if (kind == K_BAD) {
+        const int n = (int)(e & 15);
+        br.buf >>= n;
+        br.cnt -= n;
+        return -2;
+    }
     int n = (int)(e & 15), x = (int)((e >> 4) & 15);
     uint32_t len = ((e >> 8) & 0xffff) + (uint32_t)((br.buf >> n) & ((1u << x) - 1));
     br.buf >>= n + x;
@@ -468,7 +475,12 @@ __device__ __forceinline__ int one_symbol(const Tables& T, Bits& br, Out& o, int
         de = de == E_LONG ? slow_decode(T.distc, T.dist_syms, A_DIST, br.buf, DB) : 0;
         if (de == 0) return -2;
     }
-    if ((de & (3u << 24)) == K_BAD) return -2;
+    if ((de & (3u << 24)) == K_BAD) {
+        const int dn = (int)(de & 15);
+        br.buf >>= dn;
+        br.cnt -= dn;
+        return -2;
+    }
     int dn = (int)(de & 15), dx = (int)((de >> 4) & 15);
     uint32_t d = ((de >> 8) & 0xffff) + (uint32_t)((br.buf >> dn) & ((1u << dx) - 1));
     br.buf >>= dn + dx;

@@ -105,9 +105,10 @@ def bind(path):
 
 
 def rescue(data, raw=False, expected_size=None, expected_crc=None, fill=0, no_infer=False, cr_lost=0, max_output=0,
-           lib_path=None, keep_output=True):
+           lib_path=None, keep_output=True, crs_expected=0, cr_budget=0):
     """Rescues gzip (or, raw=True, raw Deflate) bytes; returns a dict with rc, data, mask, stats,
-    pieces and notes (data and mask empty when keep_output is False)."""
+    pieces and notes (data and mask empty when keep_output is False). cr_lost, crs_expected and
+    cr_budget are gr_options' fields of those names (the search for CRs a raw stream lost)."""
     lib = bind(lib_path or gpuinflate.LIB_PATH)
     out, mask = bytearray(), bytearray()
     calls = [0, 0]
@@ -121,7 +122,7 @@ def rescue(data, raw=False, expected_size=None, expected_crc=None, fill=0, no_in
         return 0
 
     cb = SINK(sink)
-    opt = Options(ctypes.sizeof(Options), fill, 1 if no_infer else 0, cr_lost, 0, max_output, 0)
+    opt = Options(ctypes.sizeof(Options), fill, 1 if no_infer else 0, cr_lost, crs_expected, max_output, cr_budget)
     res = ctypes.c_void_p()
     if raw:
         size = 0xFFFFFFFFFFFFFFFF if expected_size is None else expected_size

@@ -194,7 +194,8 @@ GI_API int gi_crc32_device_noalloc(int device, const void* d_data, uint64_t size
 typedef struct {
     const char* name;   /* the entry's path: its pax path, else its GNU long name, else its header's
                            (a ustar prefix joined to it); valid until gi_tar_free */
-    uint64_t header;    /* offset of its header in the archive */
+    uint64_t header;    /* offset of its own header in the archive (after any long-name or pax
+                           entries that name it, as the tar crate's raw_header_position) */
     uint64_t offset;    /* offset of its data */
     uint64_t size;      /* bytes of data */
     uint32_t type;      /* its typeflag byte: '0' or 0 a file, '5' a folder, '1'/'2' links, ... */

@@ -13,8 +13,9 @@
  * four calls of a process run at once (each on a rescue slot of its own: its stream, the device
  * blocks it keeps for its next call, its host tables), further calls wait for a free slot.
  *
- * Not done here (the call behaves as with the option that turns it off): the search for the CRs
- * a Windows-to-Unix transfer removed from a raw stream with its own CRC (cr_restored is 0). */
+ * The search for the CRs a Windows-to-Unix transfer removed from a raw stream with a known size
+ * and CRC (gr_rescue_raw) runs its trial decodes on the GPU, thousands in one launch, and counts
+ * the input bytes it decoded as the reference does, so that the budget cuts it at the same trial. */
 #ifndef GZRESCUE_GB300_H
 #define GZRESCUE_GB300_H
 
@@ -44,9 +45,9 @@ typedef struct {
     uint8_t fill;          /* written where a byte is unknown */
     uint8_t no_infer;      /* 1: leave the bytes copied from lost data unknown, do not infer them */
     uint8_t cr_lost;       /* CR LF to LF transfer: 0 tell from the data, 1 it happened, 2 never */
-    uint8_t crs_expected;  /* raw streams with cr_lost 1: CRs lost, when known (the search is not done) */
+    uint8_t crs_expected;  /* raw streams with cr_lost 1: CRs lost, when known (1-8; 255 none; 0 unknown) */
     uint64_t max_output;   /* GR_ERR_TOO_BIG when the output would exceed it; 0: no limit */
-    uint64_t cr_budget;    /* input bytes the CR search may decode (the search is not done) */
+    uint64_t cr_budget;    /* input bytes the CR search may decode; 0: 1 GiB */
 } gr_options;
 
 /* One piece of the output. reference: gpuinflate/rescue.h:58-66 */
@@ -72,8 +73,8 @@ typedef struct {
     uint64_t input_end;    /* byte after the last decoded block of the first member */
     uint64_t inferred_bytes;
     int32_t ascii_undone;  /* an LF to CR LF transfer was undone */
-    uint32_t cr_restored;
-    uint64_t cr_decoded;
+    uint32_t cr_restored;  /* CRs a raw stream lost in transfer that were put back */
+    uint64_t cr_decoded;   /* input bytes the search for them decoded (counted per decode) */
     int32_t hidden_damage; /* damage of a kind that can keep the decoder in step, with no CRC to vouch */
 } gr_stats;
 

@@ -53,6 +53,36 @@ int ref_inflate(const uint8_t* in, uint64_t size, uint8_t* out, uint64_t out_cap
     return 0;
 }
 
+// One gi::Decoder::run over in[0..size) (zero padded) from the state (bit, header, mode, final)
+// to stop_bit, into a buffer of `cap` symbols, stream_start `first`. res gets: status, end_bit,
+// out_len, resume.bit, resume.header, resume.mode, resume.final, blocks, symbols.
+int ref_run(const uint8_t* in, uint64_t size, uint64_t bit, uint64_t header, int mode, int final, int first,
+            uint64_t stop, uint64_t cap, uint64_t* res) {
+    static thread_local std::vector<uint8_t> buf;
+    static thread_local std::vector<uint16_t> sym;
+    static uint16_t luts[gi::LUT_U16];
+    static thread_local gi::Decoder* dec = nullptr;
+    if (!dec) {
+        dec = new gi::Decoder;
+        dec->attach(luts);
+    }
+    buf.assign((size + 3) / 4 * 4 + 64, 0);
+    if (size) memcpy(buf.data(), in, size);
+    if (sym.size() < cap) sym.resize(cap);
+    gi::Start s{bit, header, (uint8_t)mode, (int8_t)final};
+    gi::Result r = dec->run(buf.data(), size, s, nullptr, 0, sym.data(), (uint32_t)cap, first != 0, stop);
+    res[0] = (uint64_t)r.status;
+    res[1] = r.end_bit;
+    res[2] = r.out_len;
+    res[3] = r.resume.bit;
+    res[4] = r.resume.header;
+    res[5] = r.resume.mode;
+    res[6] = (uint64_t)(int64_t)r.resume.final;
+    res[7] = r.blocks;
+    res[8] = r.symbols;
+    return 0;
+}
+
 int ref_prefilter128(uint64_t v1, uint64_t v2) { return gi::header_prefilter128(v1, v2) ? 1 : 0; }
 
 int ref_plausible_dynamic_header(const uint8_t* in, uint64_t size, uint64_t bit) {
