@@ -56,7 +56,7 @@ constexpr uint32_t JOB_CHECK_REFS = 1;
 constexpr uint32_t JOB_DISCARD = 2;
 // a job whose start is known to be in step (a segment's or a stream's start): never given up
 constexpr uint32_t JOB_TRUSTED = 4;
-constexpr int32_t GIVE_UP_AFTER = 2;  // DecodeArgs.give_up of the decode paths (0 in the rescue)
+constexpr int32_t GIVE_UP_AFTER = 2;  // DecodeArgs.give_up of the segmented path (0 in batched passes and the rescue)
 constexpr uint32_t DISCARD_EXTENT = 65536 + 512;
 
 struct JobResult {
@@ -166,6 +166,10 @@ struct StoredCand {
 // UINT64_MAX where there are fewer. skip (may be null): chunks flagged nonzero are not scanned
 // (they lie inside stored blocks)
 constexpr int FIND_SLOTS_PER_CHUNK = 4;
+// per-chunk flags of launch_find's `skip` (may be NULL): a chunk wholly inside trusted stored
+// blocks (not searched); a chunk near a stream's end (final-block headers kept too)
+constexpr uint8_t SKIP_CHUNK = 1, FINAL_CHUNK = 2;
+constexpr uint64_t FINAL_TAIL_BITS = (256ull << 10) * 8;  // how near: the last 256 KiB of a stream's input
 int launch_find(const uint8_t* d_in, uint64_t bit_lo, uint64_t bit_hi, uint64_t end_word, uint32_t chunk_bits,
                 uint64_t nchunks, uint64_t* d_first, uint64_t end_bit, const uint8_t* skip, void* stream);
 // every position in (bit_lo, bit_hi) that passes the full dynamic-header check, appended to out

@@ -190,7 +190,9 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
         uint64_t hi = cb + chunk_bits < bit_hi ? cb + chunk_bits : bit_hi;
         int nfound = 0;
         uint64_t found = UINT64_MAX;  // lane j < FIND_SLOTS holds hit j
-        if (lo < hi && !(skip && skip[c])) {
+        if (lo < hi && !(skip && (skip[c] & SKIP_CHUNK))) {
+            // a chunk near the end of a stream also keeps headers of a final block (BFINAL 1)
+            const bool finals = ALL || (skip && (skip[c] & FINAL_CHUNK));
             const uint64_t w0 = lo >> 5, w1 = (hi + 31) >> 5;
             int nlist = 0;
             // verifies list[0 .. n) in batches of 32 (n a multiple of 32 unless final), keeping the
@@ -233,9 +235,10 @@ __global__ void __launch_bounds__(FIND_WARPS * 32) k_find(const uint32_t* __rest
                     uint64_t m = ~(lo64 >> 1) & (lo64 >> 2);                          // BTYPE = 2
                     m &= ~((lo64 >> 4) & (lo64 >> 5) & (lo64 >> 6) & (lo64 >> 7));    // HLIT <= 29
                     m &= ~((lo64 >> 9) & (lo64 >> 10) & (lo64 >> 11) & (lo64 >> 12)); // HDIST <= 29
-                    // BFINAL = 0 for the decode paths: only a stream's last block is final, and the
-                    // decoder before it reaches it in step (the rescue keeps every header)
-                    if (!ALL) m &= ~lo64;
+                    // BFINAL = 0 for the decode paths: only a stream's last block is final, so
+                    // final-block headers are looked for only near a stream's end (the rescue keeps
+                    // every header)
+                    if (!finals) m &= ~lo64;
                     mask = (uint32_t)m;
                     uint64_t base = wi * 32;
                     if (base < lo) mask &= ~0u << (uint32_t)(lo - base);
