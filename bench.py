@@ -914,6 +914,12 @@ def main():
         step()
         torch.cuda.synchronize()
         return
+    # the context's autotuner tries its candidate settings on the first calls of a kind of stream:
+    # those calls come before the warm-up, untimed
+    for _ in range(8):
+        _, prof = step()
+        if prof.tuned:
+            break
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -970,6 +976,10 @@ def main():
             if rc != 0 or stats.out_size != info["size"]:
                 raise RuntimeError(f"e2e failed: {rc} {lib.gi_last_error(g.ctx)}")
 
+        for _ in range(8):  # the autotuner's calls for this kind of stream (a gzip member: its ISIZE known)
+            e2e_step()
+            if g.last_profile().tuned:
+                break
         for _ in range(max(1, args.warmup)):
             e2e_step()
         torch.cuda.synchronize()
