@@ -31,11 +31,17 @@ import subprocess
 import sys
 import threading
 import time
+import zlib
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "decompressed GB/s, one 4 GiB gzip member (mixed content), 1 GB300"
+METRIC_TEXT = "decompressed GB/s, one 64 MiB gzip member (log text), 1 GB300"
+
+
+def metric_of(args):
+    return METRIC_TEXT if args.workload == "text" else METRIC
 CACHE = os.environ.get("GI_BENCH_CACHE", "/tmp/gpuzip_gb300_bench")
 
 
@@ -184,12 +190,18 @@ def cpu_candidates(body, sample, ratio, threads):
     return res
 
 
-def cpu_line(res, sample_mb, extra=""):
+def cpu_sample(args, info):
+    """Output bytes the CPU baselines decode: the first cpu_sample_mb MiB, or the whole stream."""
+    return min(args.cpu_sample_mb << 20, info["size"])
+
+
+def cpu_line(res, sample, extra=""):
     """The cpu_baseline object: the fastest of the candidates, with all of them listed."""
     best = min(res, key=lambda k: res[k]["seconds"])
-    gbs = {k: round((sample_mb << 20) / v["seconds"] / 1e9, 4) for k, v in res.items()}
+    gbs = {k: round(sample / v["seconds"] / 1e9, 4) for k, v in res.items()}
+    what = f"first {sample >> 20} MiB of output" if sample % (1 << 20) == 0 else f"all {sample} bytes of output"
     return {"value": gbs[best], "unit": "GB/s", "cores": res[best]["cores"], "kind": "port",
-            "sample": f"first {sample_mb} MiB of output of the same stream{extra}; the fastest of: the oracle port of the "
+            "sample": f"{what} of the same stream{extra}; the fastest of: the oracle port of the "
                       "reference's sequential gi::Decoder (1 thread), the port of its multi-threaded speculative CPU "
                       f"decoder (cpu_speculative, {os.cpu_count()} threads), system zlib (1 thread); this one: {best}",
             "candidates_gbs": gbs, "best": best}
@@ -199,7 +211,7 @@ def run_reference(args, member, info, ws, rank):
     if rank != 0:
         return
     body = member[10:10 + info["deflate_size"]]
-    sample = args.cpu_sample_mb << 20
+    sample = cpu_sample(args, info)
     threads = os.cpu_count() or 1
     res = cpu_candidates(body, sample, info["size"] / info["deflate_size"], threads)
     best = min(res, key=lambda k: res[k]["seconds"])
@@ -213,10 +225,10 @@ def run_reference(args, member, info, ws, rank):
         times.append(time.perf_counter() - t)
     tot = sum(times)
     value = args.steps * sample / tot / 1e9
-    cpu = cpu_line(res, args.cpu_sample_mb)
+    cpu = cpu_line(res, sample)
     cpu["value"] = round(value, 4)
     line = {
-        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "GB/s", "n_gpus": ws,
+        "impl": "reference", "metric": metric_of(args), "value": round(value, 4), "unit": "GB/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot / args.steps * 1e3, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": config_of(args, info), "cpu_baseline": cpu,
@@ -837,10 +849,35 @@ def run_rescue(args, ws, rank, local):
 
 
 def config_of(args, info):
-    return {"workload": f"one gzip member, {args.nseg} x 1 MiB segments of mixed content (seed {args.seed}), levels 1/6/9 "
-                        "changed by deflateParams inside one Deflate stream (no sync flush)",
-            "output_bytes": info["size"], "compressed_bytes": info["deflate_size"],
+    if args.workload == "text":
+        what = "one gzip member of 64 MiB of log text (seed 1), level 6"
+    else:
+        what = (f"one gzip member, {args.nseg} x 1 MiB segments of mixed content (seed {args.seed}), levels 1/6/9 "
+                "changed by deflateParams inside one Deflate stream (no sync flush)")
+    return {"workload": what, "output_bytes": info["size"], "compressed_bytes": info["deflate_size"],
             "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas"}
+
+
+def text_workload():
+    """(member bytes, info) of the 64 MiB log-text member (seed 1), cached on local disk."""
+    from gpuzip_gb300 import workloads as W
+
+    os.makedirs(CACHE, exist_ok=True)
+    path = os.path.join(CACHE, "text_s1_64m.gz")
+    meta = path + ".json"
+    if os.path.exists(path) and os.path.exists(meta):
+        with open(meta) as f:
+            info = json.load(f)
+        with open(path, "rb") as f:
+            return f.read(), info
+    member, text = W.single_text_member(seed=1)
+    info = {"crc": zlib.crc32(text), "size": len(text), "deflate_size": len(member) - 18}
+    with open(path + ".tmp", "wb") as f:
+        f.write(member)
+    os.replace(path + ".tmp", path)
+    with open(meta, "w") as f:
+        json.dump(info, f)
+    return member, info
 
 
 def main():
@@ -856,7 +893,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="one device-resident decode, no timing (for ncu)")
-    ap.add_argument("--workload", default="member", choices=["member", "batch", "serve", "bgzf", "rescue"])
+    ap.add_argument("--workload", default="member", choices=["member", "text", "batch", "serve", "bgzf", "rescue"])
     ap.add_argument("--rescue-files", type=int, default=2000, help="rescue: files in the .tar.gz")
     ap.add_argument("--nstreams", type=int, default=10000)
     ap.add_argument("--batch-total", type=float, default=8e9)
@@ -881,7 +918,7 @@ def main():
     if args.workload == "batch":
         run_batch(args, ws, rank, local)
         return
-    member, info = workload(args.seed, args.nseg)
+    member, info = text_workload() if args.workload == "text" else workload(args.seed, args.nseg)
     if args.impl == "reference":
         run_reference(args, member, info, ws, rank)
         return
@@ -958,7 +995,7 @@ def main():
     peak, peak_kind = peaks()
     achieved = alg_bytes / per_launch_s / 1e9
     roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "peak_kind": peak_kind, "traffic": traffic_per_launch(top),
+                "frac": round(achieved / peak, 5), "peak_kind": peak_kind, "traffic": traffic_per_launch(top) if args.workload == "member" else None,
                 "algorithmic_bytes_per_launch": int(alg_bytes), "launch_ms": round(per_launch_s * 1e3, 3),
                 "kernel_share": {k: round(v / sum(kms.values()), 4) for k, v in kms.items()}}
     gpu_launches = sum(p["launches"] for p in profs)
@@ -1003,11 +1040,12 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         body = member[10:10 + info["deflate_size"]]
-        res = cpu_candidates(body, args.cpu_sample_mb << 20, info["size"] / info["deflate_size"], os.cpu_count() or 1)
-        cpu = cpu_line(res, args.cpu_sample_mb)
+        sample = cpu_sample(args, info)
+        res = cpu_candidates(body, sample, info["size"] / info["deflate_size"], os.cpu_count() or 1)
+        cpu = cpu_line(res, sample)
     if rank == 0:
         line = {
-            "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+            "metric": metric_of(args), "value": round(value, 3), "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total_s / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": config_of(args, info),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
