@@ -209,11 +209,16 @@ struct SpanDesc {
 // fills piece0/npiece of every span (spans and pieces both sorted, the pieces back to back)
 void span_pieces(SpanDesc* spans, uint64_t nspans, const Piece* pieces, uint64_t npieces);
 // passes: 1 = local resolution (and the check for matches before the start), 2 = windows and bytes.
-// One stream in spans of SPAN (the first with W bytes of seg_window before it):
+// One stream in spans of span_len bytes (a power of two from 64 KiB to SPAN; the first span with W
+// bytes of seg_window before it):
 // work: one word of device memory the launch uses as the span queue of k_local
 int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans, uint64_t nspans,
-                   uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad,
-                   uint8_t* out, int passes, unsigned* work, void* stream);
+                   uint64_t span_len, uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16,
+                   uint8_t* windows, int* bad, uint8_t* out, int passes, unsigned* work, void* stream);
+// the spans of one stream of `total` output bytes: SPAN, halved (not below 64 KiB, twice a window)
+// while the stream has fewer spans than the GPU has SMs, so a small stream's spans are resolved on
+// as many blocks as its decode ran on
+uint64_t span_length(uint64_t total);
 // Many streams (every stream starting at its first span, W 0). A stream of fewer than
 // GROUPED_SPANS spans (but more than one) is listed in multi as (first span, span count); a longer
 // one is cut into groups of consecutive spans (about the square root of its span count each),

@@ -786,9 +786,15 @@ static unsigned local_grid(uint64_t nspans) {
     return (unsigned)(nspans < g ? nspans : g);
 }
 
+uint64_t span_length(uint64_t total) {
+    uint64_t s = SPAN;
+    while (s > (64u << 10) && (total + s - 1) / s < (uint64_t)sm_count()) s >>= 1;
+    return s;
+}
+
 int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const SpanDesc* spans, uint64_t nspans,
-                   uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16, uint8_t* windows, int* bad,
-                   uint8_t* out, int passes, unsigned* work, void* stream) {
+                   uint64_t span_len, uint64_t total, uint32_t W, const uint8_t* seg_window, uint16_t* out16,
+                   uint8_t* windows, int* bad, uint8_t* out, int passes, unsigned* work, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (!total || npieces <= 0) return 0;
     int launches = 0;
@@ -801,18 +807,18 @@ int launch_resolve(const uint16_t* pool, const Piece* pieces, int npieces, const
         launches++;
     }
     if (passes & 2) {
-        // one stream, spans of SPAN: groups of L spans, L about sqrt(spans) balances the three phases
+        // one stream, spans of span_len: groups of L spans, L about sqrt(spans) balances the three phases
         uint64_t L = 1;
         while (L * L < nspans) L++;
         uint64_t ngroups = (nspans + L - 1) / L;
         uint64_t nmaps = nspans - 1;  // M_s for s < nspans - 1
         uint16_t* maps = out16 + ((total + 63) & ~63ull);
         if (nmaps) {
-            k_compose<<<(unsigned)((nmaps + L - 1) / L), WT, 2 * WINDOW, st>>>(out16, nmaps, SPAN, L, maps);
+            k_compose<<<(unsigned)((nmaps + L - 1) / L), WT, 2 * WINDOW, st>>>(out16, nmaps, span_len, L, maps);
             launches++;
         }
         k_chain<<<1, WT, 0, st>>>(maps, ngroups, L, nspans, seg_window, W, windows);
-        k_fill<<<(unsigned)ngroups, WT, 0, st>>>(out16, nspans, SPAN, L, windows);
+        k_fill<<<(unsigned)ngroups, WT, 0, st>>>(out16, nspans, span_len, L, windows);
         uint64_t fgrid = nspans < (uint64_t)nsm * 8 ? nspans : (uint64_t)nsm * 8;
         k_final<<<(unsigned)fgrid, 256, 0, st>>>(out16, spans, nspans, windows, out);
         launches += 3;
