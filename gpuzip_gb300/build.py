@@ -36,7 +36,7 @@ def build(verbose=False, ptxas_info=False):
         obj = os.path.join(bdir, src.replace(".cu", ".o"))
         srcp = os.path.join(CSRC, src)
         deps = [srcp, os.path.join(ROOT, "include", "gpuinflate.h"), os.path.join(ROOT, "include", "gzrescue_gb300.h")] + [
-            os.path.join(CSRC, h) for h in ("gi_common.cuh", "gi_internal.h", "gi_arena.h", "gi_find_cl.h", "gi_tar.h", "gi_model.h")]
+            os.path.join(CSRC, h) for h in ("gi_common.cuh", "gi_internal.h", "gi_arena.h", "gi_find_cl.h", "gi_tar.h", "gi_model.h", "gi_parallel.h")]
         if not ptxas_info and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
             return obj, ""
         r = subprocess.run([cc, "-c", srcp, "-o", obj] + flags, capture_output=True, text=True)
