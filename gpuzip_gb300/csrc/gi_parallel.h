@@ -49,7 +49,13 @@ void parallel_for(size_t n, size_t per_thread, F&& fn, size_t work = SIZE_MAX) {
     };
     std::vector<std::thread> th;
     th.reserve(nt - 1);
-    for (size_t t = 1; t < nt; t++) th.emplace_back(run);
+    for (size_t t = 1; t < nt; t++) {
+        try {
+            th.emplace_back(run);
+        } catch (...) {  // no thread to be had: the caller takes the slices the others would have
+            break;
+        }
+    }
     run();
     for (std::thread& t : th) t.join();
 }
