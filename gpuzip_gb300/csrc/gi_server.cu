@@ -415,6 +415,7 @@ GI_API int gi_server_create(const gi_server_config* cfg, gi_done done, void* use
     s->user = user;
     s->t0 = clk::now();
     size_t free0 = 0, free1 = 0, total = 0;
+    gr_release_cached();  // device blocks kept by rescues before the server: its budget is its own
     cudaMemGetInfo(&free0, &total);
     for (uint32_t w = 0; w < c.workers; w++) {
         gi_config gc{sizeof(gi_config), c.device, pass_mb, 0};

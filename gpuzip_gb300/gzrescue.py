@@ -14,7 +14,7 @@ GR_UNKNOWN, GR_EXACT, GR_SUSPECT, GR_INFERRED = range(4)
 
 EXPORTED = ("gr_abi_version", "gr_rescue", "gr_rescue_raw", "gr_result_stats", "gr_result_pieces", "gr_result_notes",
             "gr_free", "gr_last_launches", "gr_rescue_tar", "gr_tar_result_stats", "gr_tar_result_files",
-            "gr_tar_result_skipped", "gr_tar_free")
+            "gr_tar_result_skipped", "gr_tar_free", "gr_release_cached")
 TAR_INTACT, TAR_SUSPECT, TAR_PARTIAL, TAR_INFERRED, TAR_UNVERIFIED = range(5)
 
 
@@ -88,6 +88,9 @@ def bind(path):
     lib.gr_free.restype = None
     if hasattr(lib, "gr_last_launches"):
         lib.gr_last_launches.restype = ctypes.c_uint64
+    if hasattr(lib, "gr_release_cached"):
+        lib.gr_release_cached.argtypes = []
+        lib.gr_release_cached.restype = None
     if hasattr(lib, "gr_rescue_tar"):
         lib.gr_rescue_tar.argtypes = [ctypes.c_char_p, u64, ctypes.POINTER(Options), SINK, vp, ctypes.POINTER(vp),
                                       ctypes.POINTER(vp)]

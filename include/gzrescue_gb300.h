@@ -106,6 +106,13 @@ GR_API void gr_free(gr_result* r);
  * gr_rescue_raw call of the process launched. */
 GR_API uint64_t gr_last_launches(void);
 
+/* Added here, no counterpart in the reference: frees the device blocks the rescue slots keep for
+ * their next call. Between calls a slot keeps the blocks its last call used, up to a fifth of the
+ * device's memory (all slots together up to half of it): a large file's resolve holds 8 bytes per
+ * output byte, which costs tens of milliseconds to allocate and free per call. Slots in use by a
+ * call keep theirs. The library's decoder calls this itself when a device allocation fails. */
+GR_API void gr_release_cached(void);
+
 /* ---- Added here: the tar walk over the rescued output, on the GPU where it lies.
  * gpuzip's Rust host reads a rescued .tar.gz with its TarReader (src/rescue.rs:374-829) and then
  * applies two rules (src/main.rs:546-558): these give the same outcome for the stream gr_rescue

@@ -110,3 +110,9 @@ def test_bad_arguments_without_gpu(lib):
     assert lib.gr_tar_result_files(None, None) == 0 and lib.gr_tar_result_skipped(None, None) == 0
     assert not lib.gr_tar_result_stats(None)
     lib.gr_tar_free(None)
+
+
+def test_release_cached_without_gpu(lib):
+    """With no rescue run, no slot keeps a block: the call returns without touching the device."""
+    lib.gr_release_cached()
+    lib.gr_release_cached()
