@@ -72,3 +72,25 @@ def test_tar_walk_matches_reader(case):
     want = case["reference"]["tar"]
     got = {k: r["tar"][k] for k in want}
     assert got == want
+
+
+def test_inference_model_learned_on_gpu(capfd, monkeypatch):
+    """The inference cases' context models are learned on the GPU (atomic insertion, checked to
+    give the ordered table's counts), not again on the host: the debug report names the learner,
+    and the results are the reference's."""
+    monkeypatch.setenv("GPUZIP_RESCUE_DEBUG", "1")
+    for case in CASES:
+        _, r = G.run_case(case["name"], case["base"], [tuple(o) for o in case["ops"]], BASES, INFO, None, no_infer=False)
+        assert not compare(case["name"], G.describe(r), case["reference_infer"])
+    err = capfd.readouterr().err
+    assert "train(gpu)" in err and "train(host)" not in err
+
+
+def test_inference_in_small_chunks_matches_reference(monkeypatch):
+    """The inference's host pass over the list of unknown bytes, cut into chunks of 16 entries
+    (so that even the small cases take many chunks and owners in parallel): the same results."""
+    monkeypatch.setenv("GPUZIP_RESCUE_CHUNK", "16")
+    for case in CASES:
+        _, r = G.run_case(case["name"], case["base"], [tuple(o) for o in case["ops"]], BASES, INFO, None, no_infer=False)
+        diffs = compare(case["name"], G.describe(r), case["reference_infer"])
+        assert not diffs, (case["name"], diffs[:12])
